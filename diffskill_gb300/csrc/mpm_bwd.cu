@@ -1,0 +1,113 @@
+// Adjoint launchers: one substep's adjoint (grid recompute, g2p.grad,
+// grid_op.grad, p2g.grad) and the soft-contact adjoint.
+#include "mpm_kernels.cuh"
+#include "mpm_launch.h"
+
+namespace mpm {
+
+template <typename T>
+Consts<T> make_consts(const LaunchCtx& L);  // mpm_fwd.cu
+
+static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+template <typename T, typename S>
+cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* g1, T* g0, const double* pose_f,
+                               const double* pose_f1, double* g_pose_f, double* g_pose_f1) {
+  Consts<T> c = make_consts<T>(L);
+  const int64_t nodes = (int64_t)c.n_scenes * c.G;
+  Node<T>* gin = (Node<T>*)L.grid_a;
+  Node<T>* gout = (Node<T>*)L.grid_b;
+  Node<T>* g_gin = (Node<T>*)L.grid_c;
+  Node<T>* g_gout = (Node<T>*)L.grid_d;
+  const unsigned pb = blocks_for(c.n_particles, 128);
+  // recompute the grid of this substep (substep_grad, mpm_simulator.py:327-333)
+  cudaError_t e = cudaMemsetAsync(gin, 0, nodes * sizeof(Node<T>), L.stream);
+  if (e != cudaSuccess) return e;
+  if (c.n_particles > 0) {
+    k_p2g<T, S><<<pb, 128, 0, L.stream>>>(c, st0, (T*)nullptr, L.pscene, gin);
+    ++*L.launches;
+  }
+  k_grid_op<T><<<(unsigned)(nodes / 128), 128, 0, L.stream>>>(c, gin, gout, L.tools, L.tool_off, pose_f, pose_f1);
+  ++*L.launches;
+  e = cudaMemsetAsync(g_gout, 0, nodes * sizeof(Node<T>), L.stream);
+  if (e != cudaSuccess) return e;
+  if (c.n_particles > 0) {
+    k_g2p_adj<T><<<pb, 128, 0, L.stream>>>(c, st0, g1, g0, L.pscene, gout, g_gout);
+    ++*L.launches;
+  }
+  k_grid_op_adj<T><<<(unsigned)(nodes / 128), 128, 0, L.stream>>>(c, gin, g_gout, g_gin, L.tools, L.tool_off, pose_f,
+                                                                  pose_f1, g_pose_f, g_pose_f1);
+  ++*L.launches;
+  if (c.n_particles > 0) {
+    k_p2g_adj<T, S><<<pb, 128, 0, L.stream>>>(c, st0, g1, g0, L.pscene, g_gin);
+    ++*L.launches;
+  }
+  return cudaGetLastError();
+}
+
+// soft contact adjoint (loss.py:143-162 differentiated)
+template <typename T>
+__global__ void __launch_bounds__(128) k_contact_adj(Consts<T> c, const T* __restrict__ st,
+                                                     const int* __restrict__ pscene,
+                                                     const MpmToolDesc* __restrict__ tools,
+                                                     const int* __restrict__ tool_off,
+                                                     const double* __restrict__ pose,
+                                                     const double* __restrict__ sums,
+                                                     const double* __restrict__ g_min, T* __restrict__ gst,
+                                                     double* __restrict__ g_pose) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= c.n_particles) return;
+  int sc = pscene[p];
+  T x[3];
+  load_row(st, c.ld, p, 0, 3, x);
+  T gx[3] = {T(0), T(0), T(0)};
+  for (int t = tool_off[sc]; t < tool_off[sc + 1]; ++t) {
+    if (tools[t].action_dim <= 0 || g_min[t] == 0.0) continue;
+    Tool<T> tl;
+    Pose<T> P;
+    to_tool(tools[t], tl);
+    to_pose(pose + 8 * t, P);
+    T sd = tool_sdf(tl, P, x);
+    if (!(T(0) < sd)) continue;
+    double norm = sums[2 * t], md = sums[2 * t + 1] / norm;
+    double d = double(sd), w = 1.0 / (1.0 + d * d * 10000.0);
+    double g_norm = -g_min[t] * md / norm;
+    double g_w = g_min[t] * d / norm + g_norm;
+    double g_d = g_min[t] * w / norm + g_w * (-2e4 * d * w * w);
+    PoseGrad<T> gP;
+    gP.zero();
+    tool_sdf_vjp(tl, P, x, T(g_d), gx, gP);
+    const T* gv = &gP.pos[0];
+    for (int k = 0; k < 3; ++k) atomicAdd(g_pose + 8 * t + k, double(gv[k]));
+    for (int k = 0; k < 4; ++k) atomicAdd(g_pose + 8 * t + 3 + k, double(gP.rot[k]));
+    atomicAdd(g_pose + 8 * t + 7, double(gP.gap));
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) gst[(int64_t)d * c.ld + p] += gx[d];
+}
+
+template <typename T>
+cudaError_t launch_soft_contact_bwd(const LaunchCtx& L, int n_tools, const T* st, const double* pose,
+                                    const double* sums, const double* g_min, T* gst, double* g_pose) {
+  (void)n_tools;
+  Consts<T> c = make_consts<T>(L);
+  if (c.n_particles > 0) {
+    k_contact_adj<T><<<blocks_for(c.n_particles, 128), 128, 0, L.stream>>>(c, st, L.pscene, L.tools, L.tool_off,
+                                                                             pose, sums, g_min, gst, g_pose);
+    ++*L.launches;
+  }
+  return cudaGetLastError();
+}
+
+#define MPM_INST_BWD(T, S)                                                                                  \
+  template cudaError_t launch_substep_bwd<T, S>(const LaunchCtx&, const T*, const T*, T*, const double*, \
+                                                const double*, double*, double*);
+MPM_INST_BWD(float, float)
+MPM_INST_BWD(float, double)
+MPM_INST_BWD(double, double)
+template cudaError_t launch_soft_contact_bwd<float>(const LaunchCtx&, int, const float*, const double*, const double*,
+                                                    const double*, float*, double*);
+template cudaError_t launch_soft_contact_bwd<double>(const LaunchCtx&, int, const double*, const double*,
+                                                     const double*, const double*, double*, double*);
+
+}  // namespace mpm

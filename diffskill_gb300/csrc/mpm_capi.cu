@@ -1,0 +1,483 @@
+// C ABI of the GB300 MPM substep (include/mpm_gb300.h): handle lifetime,
+// argument checks, precision dispatch, and the tool-kinematics kernels.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "mpm_launch.h"
+#include "mpm_math.cuh"
+#include "mpm_tools.cuh"
+
+struct MpmHandle {
+  MpmParams p;
+  int device = -1;
+  int64_t G = 0;
+  std::vector<int64_t> offsets;
+  int* d_pscene = nullptr;
+  int* d_tool_off = nullptr;
+  MpmToolDesc* d_tools = nullptr;
+  int n_tools = 0;
+  std::vector<MpmToolDesc> h_tools;
+  unsigned int* d_status = nullptr;
+  void* grid[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::string err;
+  int64_t launches = 0;
+};
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_create_err;
+
+int fail(MpmHandle* h, int code, const std::string& msg) {
+  if (h) {
+    h->err = msg;
+  } else {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_create_err = msg;
+  }
+  return code;
+}
+int cuda_fail(MpmHandle* h, cudaError_t e, const char* where) {
+  return fail(h, MPM_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+size_t real_size(int precision) { return precision == MPM_PREC_FP64 ? sizeof(double) : sizeof(float); }
+
+mpm::LaunchCtx ctx(MpmHandle* h, void* stream) {
+  mpm::LaunchCtx L;
+  L.p = &h->p;
+  L.G = h->G;
+  L.pscene = h->d_pscene;
+  L.tools = h->d_tools;
+  L.tool_off = h->d_tool_off;
+  L.status = h->d_status;
+  L.grid_a = h->grid[0];
+  L.grid_b = h->grid[1];
+  L.grid_c = h->grid[2];
+  L.grid_d = h->grid[3];
+  L.stream = (cudaStream_t)stream;
+  L.launches = &h->launches;
+  return L;
+}
+int check_device(MpmHandle* h) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaGetDevice");
+  if (dev != h->device)
+    return fail(h, MPM_E_INVALID, "handle was created on device " + std::to_string(h->device) +
+                                      " but device " + std::to_string(dev) + " is current");
+  return MPM_OK;
+}
+int check_aligned(MpmHandle* h, const void* ptr, const char* name, bool allow_null = false) {
+  if (!ptr) return allow_null ? MPM_OK : fail(h, MPM_E_INVALID, std::string(name) + " is NULL");
+  if (((uintptr_t)ptr) % 16 != 0) return fail(h, MPM_E_INVALID, std::string(name) + " is not 16-byte aligned");
+  return MPM_OK;
+}
+#define MPM_TRY(x)          \
+  do {                      \
+    int _rc = (x);          \
+    if (_rc != MPM_OK) return _rc; \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// tool kinematics (FP64): set_velocity + forward_kinematics per action
+// ---------------------------------------------------------------------------
+__device__ void fk_step(const MpmToolDesc& d, const double* p0, const double* vv, double* p1) {
+  for (int k = 0; k < 3; ++k) {
+    double a = p0[k] + vv[k];
+    double mn = (a < d.upper[k]) ? a : d.upper[k];
+    p1[k] = (d.lower[k] < mn) ? mn : d.lower[k];
+  }
+  double wq[4];
+  mpm::w2quat(vv + 3, wq);
+  if (d.type == mpm::TOOL_GRIPPER) {
+    mpm::qmul(p0 + 3, wq, p1 + 3);  // Gripper: rotation[f] * w2quat(w) (primitives.py:460)
+    double a = p0[7] - vv[6];
+    double mx = (d.min_gap < a) ? a : d.min_gap;
+    p1[7] = (mx < d.max_gap) ? mx : d.max_gap;
+  } else {
+    mpm::qmul(wq, p0 + 3, p1 + 3);  // w2quat(w) * rotation[f] (primive_base.py:156)
+    p1[7] = p0[7];
+  }
+}
+__device__ void action_velocity(const MpmToolDesc& d, const double* a, int n_sub, double* vv) {
+  for (int k = 0; k < 8; ++k) vv[k] = 0.0;
+  if (d.action_dim <= 0) return;
+  for (int k = 0; k < 3; ++k) vv[k] = a[k] * d.action_scale[k] / n_sub;
+  if (d.action_dim > 3)
+    for (int k = 0; k < 3; ++k) vv[3 + k] = a[3 + k] * d.action_scale[3 + k] / n_sub;
+  if (d.type == mpm::TOOL_GRIPPER) vv[6] = a[6] * d.action_scale[6] / n_sub;
+}
+__global__ void k_tools_action(const MpmToolDesc* __restrict__ tools, int n_tools, const double* __restrict__ action,
+                               double* __restrict__ vel, double* __restrict__ pose, int n_sub) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tools) return;
+  const MpmToolDesc d = tools[t];
+  double vv[8];
+  action_velocity(d, action + 8 * t, n_sub, vv);
+  for (int j = 0; j < n_sub; ++j) {
+    for (int k = 0; k < 8; ++k) vel[((int64_t)j * n_tools + t) * 8 + k] = vv[k];
+    fk_step(d, pose + ((int64_t)j * n_tools + t) * 8, vv, pose + ((int64_t)(j + 1) * n_tools + t) * 8);
+  }
+}
+__global__ void k_tools_action_bwd(const MpmToolDesc* __restrict__ tools, int n_tools, const double* __restrict__ vel,
+                                   const double* __restrict__ pose, double* __restrict__ g_pose,
+                                   double* __restrict__ g_action, int n_sub) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tools) return;
+  const MpmToolDesc d = tools[t];
+  double gvv_sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int j = n_sub - 1; j >= 0; --j) {
+    const double* p0 = pose + ((int64_t)j * n_tools + t) * 8;
+    const double* vv = vel + ((int64_t)j * n_tools + t) * 8;
+    const double* g1 = g_pose + ((int64_t)(j + 1) * n_tools + t) * 8;
+    double* g0 = g_pose + ((int64_t)j * n_tools + t) * 8;
+    double gvv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 3; ++k) {
+      double a = p0[k] + vv[k];
+      double mn = (a < d.upper[k]) ? a : d.upper[k];
+      if ((a < d.upper[k]) && (d.lower[k] < mn)) {
+        g0[k] += g1[k];
+        gvv[k] += g1[k];
+      }
+    }
+    double wq[4], gwq[4] = {0, 0, 0, 0};
+    mpm::w2quat(vv + 3, wq);
+    if (d.type == mpm::TOOL_GRIPPER) {
+      mpm::qmul_vjp(p0 + 3, wq, g1 + 3, g0 + 3, gwq);
+      double a = p0[7] - vv[6];
+      double mx = (d.min_gap < a) ? a : d.min_gap;
+      if ((d.min_gap < a) && (mx < d.max_gap)) {
+        g0[7] += g1[7];
+        gvv[6] -= g1[7];
+      }
+    } else {
+      mpm::qmul_vjp(wq, p0 + 3, g1 + 3, gwq, g0 + 3);
+      g0[7] += g1[7];
+    }
+    mpm::w2quat_vjp(vv + 3, gwq, gvv + 3);
+    for (int k = 0; k < 8; ++k) gvv_sum[k] += gvv[k];
+  }
+  // set_velocity.grad: v = a * scale / n_sub for every substep of the action
+  if (d.action_dim > 0) {
+    for (int k = 0; k < 3; ++k) g_action[8 * t + k] += gvv_sum[k] * d.action_scale[k] / n_sub;
+    if (d.action_dim > 3)
+      for (int k = 0; k < 3; ++k) g_action[8 * t + 3 + k] += gvv_sum[3 + k] * d.action_scale[3 + k] / n_sub;
+    if (d.type == mpm::TOOL_GRIPPER) g_action[8 * t + 6] += gvv_sum[6] * d.action_scale[6] / n_sub;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mpm_version(void) { return "mpm_gb300 1 (sm_103a)"; }
+
+int mpm_create(const MpmParams* params, const int64_t* scene_offsets, MpmHandle** out) {
+  if (!params || !scene_offsets || !out) return fail(nullptr, MPM_E_INVALID, "mpm_create: NULL argument");
+  *out = nullptr;
+  const MpmParams& p = *params;
+  if (p.abi_version != MPM_ABI_VERSION)
+    return fail(nullptr, MPM_E_INVALID, "mpm_create: ABI version mismatch (got " + std::to_string(p.abi_version) +
+                                            ", library " + std::to_string(MPM_ABI_VERSION) + ")");
+  if (p.precision < MPM_PREC_FP32 || p.precision > MPM_PREC_FP64)
+    return fail(nullptr, MPM_E_INVALID, "mpm_create: unknown precision " + std::to_string(p.precision));
+  if (p.n_grid < 8 || p.n_grid > 1024 || p.n_grid % 8 != 0)
+    return fail(nullptr, MPM_E_INVALID, "mpm_create: n_grid must be a multiple of 8 in [8, 1024], got " +
+                                            std::to_string(p.n_grid));
+  if (p.n_scenes < 1) return fail(nullptr, MPM_E_INVALID, "mpm_create: n_scenes must be >= 1");
+  if (p.n_particles < 0 || p.ld < p.n_particles || p.n_particles > (int64_t)INT32_MAX * 2)
+    return fail(nullptr, MPM_E_INVALID, "mpm_create: need 0 <= n_particles <= ld");
+  if (!(p.dt > 0) || !(p.dx > 0) || !(p.p_mass > 0))
+    return fail(nullptr, MPM_E_INVALID, "mpm_create: dt, dx and p_mass must be positive");
+  if (scene_offsets[0] != 0 || scene_offsets[p.n_scenes] != p.n_particles)
+    return fail(nullptr, MPM_E_INVALID, "mpm_create: scene_offsets must start at 0 and end at n_particles");
+  for (int s = 0; s < p.n_scenes; ++s)
+    if (scene_offsets[s + 1] < scene_offsets[s])
+      return fail(nullptr, MPM_E_INVALID, "mpm_create: scene_offsets must be non-decreasing");
+
+  MpmHandle* h = new MpmHandle();
+  h->p = p;
+  h->G = (int64_t)p.n_grid * p.n_grid * p.n_grid;
+  h->offsets.assign(scene_offsets, scene_offsets + p.n_scenes + 1);
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e != cudaSuccess) {
+    delete h;
+    return cuda_fail(nullptr, e, "mpm_create: cudaGetDevice");
+  }
+  std::vector<int> ps(p.n_particles);
+  for (int s = 0; s < p.n_scenes; ++s)
+    for (int64_t i = scene_offsets[s]; i < scene_offsets[s + 1]; ++i) ps[i] = s;
+  std::vector<int> toff(p.n_scenes + 1, 0);
+  const size_t gbytes = (size_t)p.n_scenes * h->G * 4 * real_size(p.precision);
+  bool ok = true;
+  ok = ok && cudaMalloc(&h->d_pscene, std::max<size_t>(1, ps.size()) * sizeof(int)) == cudaSuccess;
+  ok = ok && cudaMalloc(&h->d_tool_off, toff.size() * sizeof(int)) == cudaSuccess;
+  ok = ok && cudaMalloc(&h->d_status, sizeof(unsigned int)) == cudaSuccess;
+  for (int i = 0; i < 4 && ok; ++i) ok = cudaMalloc(&h->grid[i], gbytes) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    mpm_destroy(h);
+    return fail(nullptr, MPM_E_NOMEM, "mpm_create: device allocation of " + std::to_string(4 * gbytes) +
+                                          " grid bytes failed");
+  }
+  if (!ps.empty()) e = cudaMemcpy(h->d_pscene, ps.data(), ps.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(h->d_tool_off, toff.data(), toff.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(h->d_status, 0, sizeof(unsigned int));
+  if (e != cudaSuccess) {
+    mpm_destroy(h);
+    return cuda_fail(nullptr, e, "mpm_create: upload");
+  }
+  *out = h;
+  return MPM_OK;
+}
+
+int mpm_destroy(MpmHandle* h) {
+  if (!h) return MPM_OK;
+  cudaFree(h->d_pscene);
+  cudaFree(h->d_tool_off);
+  cudaFree(h->d_tools);
+  cudaFree(h->d_status);
+  for (int i = 0; i < 4; ++i) cudaFree(h->grid[i]);
+  delete h;
+  return MPM_OK;
+}
+
+int mpm_set_tools(MpmHandle* h, const MpmToolDesc* tools, int32_t n_tools) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_set_tools: NULL handle");
+  if (n_tools < 0 || (n_tools > 0 && !tools)) return fail(h, MPM_E_INVALID, "mpm_set_tools: bad tool array");
+  MPM_TRY(check_device(h));
+  std::vector<int> toff(h->p.n_scenes + 1, 0);
+  int prev = 0;
+  for (int i = 0; i < n_tools; ++i) {
+    const MpmToolDesc& d = tools[i];
+    if (d.type < MPM_TOOL_SPHERE || d.type > MPM_TOOL_GRIPPER)
+      return fail(h, MPM_E_INVALID, "mpm_set_tools: tool " + std::to_string(i) + " has unknown type");
+    if (d.scene < 0 || d.scene >= h->p.n_scenes || d.scene < prev)
+      return fail(h, MPM_E_INVALID, "mpm_set_tools: tools must be sorted by a valid scene index");
+    if (d.action_dim < 0 || d.action_dim > 7)
+      return fail(h, MPM_E_INVALID, "mpm_set_tools: action_dim must be in [0, 7]");
+    prev = d.scene;
+    toff[d.scene + 1]++;
+  }
+  for (int s = 0; s < h->p.n_scenes; ++s) {
+    if (toff[s + 1] > mpm::MAX_TOOLS_PER_SCENE)
+      return fail(h, MPM_E_INVALID, "mpm_set_tools: more than " + std::to_string(mpm::MAX_TOOLS_PER_SCENE) +
+                                        " tools in scene " + std::to_string(s));
+    toff[s + 1] += toff[s];
+  }
+  cudaError_t e = cudaSuccess;
+  if (n_tools > h->n_tools) {
+    cudaFree(h->d_tools);
+    h->d_tools = nullptr;
+    e = cudaMalloc(&h->d_tools, n_tools * sizeof(MpmToolDesc));
+    if (e != cudaSuccess) return cuda_fail(h, e, "mpm_set_tools: cudaMalloc");
+  }
+  if (n_tools > 0) e = cudaMemcpy(h->d_tools, tools, n_tools * sizeof(MpmToolDesc), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(h->d_tool_off, toff.data(), toff.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(h, e, "mpm_set_tools: upload");
+  h->n_tools = n_tools;
+  h->h_tools.assign(tools, tools + n_tools);
+  return MPM_OK;
+}
+
+int mpm_tools_action(MpmHandle* h, const double* action, double* vel, double* pose, int32_t n_sub, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_tools_action: NULL handle");
+  if (n_sub < 1) return fail(h, MPM_E_INVALID, "mpm_tools_action: n_sub must be >= 1");
+  if (h->n_tools == 0) return MPM_OK;
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, action, "action"));
+  MPM_TRY(check_aligned(h, vel, "vel"));
+  MPM_TRY(check_aligned(h, pose, "pose"));
+  k_tools_action<<<(h->n_tools + 63) / 64, 64, 0, (cudaStream_t)stream>>>(h->d_tools, h->n_tools, action, vel, pose,
+                                                                          n_sub);
+  ++h->launches;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_tools_action");
+}
+
+int mpm_tools_action_bwd(MpmHandle* h, const double* vel, const double* pose, double* g_pose, double* g_action,
+                         int32_t n_sub, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_tools_action_bwd: NULL handle");
+  if (n_sub < 1) return fail(h, MPM_E_INVALID, "mpm_tools_action_bwd: n_sub must be >= 1");
+  if (h->n_tools == 0) return MPM_OK;
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, vel, "vel"));
+  MPM_TRY(check_aligned(h, pose, "pose"));
+  MPM_TRY(check_aligned(h, g_pose, "g_pose"));
+  MPM_TRY(check_aligned(h, g_action, "g_action"));
+  k_tools_action_bwd<<<(h->n_tools + 63) / 64, 64, 0, (cudaStream_t)stream>>>(h->d_tools, h->n_tools, vel, pose,
+                                                                              g_pose, g_action, n_sub);
+  ++h->launches;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_tools_action_bwd");
+}
+
+int mpm_substep_fwd(MpmHandle* h, const void* state_f, void* state_f1, const double* pose_f, const double* pose_f1,
+                    void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_substep_fwd: NULL handle");
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, state_f, "state_f"));
+  MPM_TRY(check_aligned(h, state_f1, "state_f1"));
+  if (state_f == state_f1) return fail(h, MPM_E_INVALID, "mpm_substep_fwd: state_f and state_f1 must differ");
+  MPM_TRY(check_aligned(h, pose_f, "pose_f", h->n_tools == 0));
+  MPM_TRY(check_aligned(h, pose_f1, "pose_f1", h->n_tools == 0));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e;
+  switch (h->p.precision) {
+    case MPM_PREC_FP32:
+      e = mpm::launch_substep_fwd<float, float>(L, (const float*)state_f, (float*)state_f1, pose_f, pose_f1);
+      break;
+    case MPM_PREC_FP32_SVD64:
+      e = mpm::launch_substep_fwd<float, double>(L, (const float*)state_f, (float*)state_f1, pose_f, pose_f1);
+      break;
+    default:
+      e = mpm::launch_substep_fwd<double, double>(L, (const double*)state_f, (double*)state_f1, pose_f, pose_f1);
+  }
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_substep_fwd");
+}
+
+int mpm_substep_bwd(MpmHandle* h, const void* state_f, const void* g_state_f1, void* g_state_f,
+                    const double* pose_f, const double* pose_f1, double* g_pose_f, double* g_pose_f1,
+                    void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_substep_bwd: NULL handle");
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, state_f, "state_f"));
+  MPM_TRY(check_aligned(h, g_state_f1, "g_state_f1"));
+  MPM_TRY(check_aligned(h, g_state_f, "g_state_f"));
+  if (g_state_f == g_state_f1) return fail(h, MPM_E_INVALID, "mpm_substep_bwd: g_state_f and g_state_f1 must differ");
+  bool nt = h->n_tools == 0;
+  MPM_TRY(check_aligned(h, pose_f, "pose_f", nt));
+  MPM_TRY(check_aligned(h, pose_f1, "pose_f1", nt));
+  MPM_TRY(check_aligned(h, g_pose_f, "g_pose_f", nt));
+  MPM_TRY(check_aligned(h, g_pose_f1, "g_pose_f1", nt));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e;
+  switch (h->p.precision) {
+    case MPM_PREC_FP32:
+      e = mpm::launch_substep_bwd<float, float>(L, (const float*)state_f, (const float*)g_state_f1, (float*)g_state_f,
+                                                pose_f, pose_f1, g_pose_f, g_pose_f1);
+      break;
+    case MPM_PREC_FP32_SVD64:
+      e = mpm::launch_substep_bwd<float, double>(L, (const float*)state_f, (const float*)g_state_f1,
+                                                 (float*)g_state_f, pose_f, pose_f1, g_pose_f, g_pose_f1);
+      break;
+    default:
+      e = mpm::launch_substep_bwd<double, double>(L, (const double*)state_f, (const double*)g_state_f1,
+                                                  (double*)g_state_f, pose_f, pose_f1, g_pose_f, g_pose_f1);
+  }
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_substep_bwd");
+}
+
+int mpm_grid_mass(MpmHandle* h, const void* state, void* grid_m, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_grid_mass: NULL handle");
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, state, "state"));
+  MPM_TRY(check_aligned(h, grid_m, "grid_m"));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e = h->p.precision == MPM_PREC_FP64
+                      ? mpm::launch_grid_mass<double>(L, (const double*)state, (double*)grid_m)
+                      : mpm::launch_grid_mass<float>(L, (const float*)state, (float*)grid_m);
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_grid_mass");
+}
+
+int mpm_grid_mass_bwd(MpmHandle* h, const void* state, const void* g_grid_m, void* g_state, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_grid_mass_bwd: NULL handle");
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, state, "state"));
+  MPM_TRY(check_aligned(h, g_grid_m, "g_grid_m"));
+  MPM_TRY(check_aligned(h, g_state, "g_state"));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e =
+      h->p.precision == MPM_PREC_FP64
+          ? mpm::launch_grid_mass_bwd<double>(L, (const double*)state, (const double*)g_grid_m, (double*)g_state)
+          : mpm::launch_grid_mass_bwd<float>(L, (const float*)state, (const float*)g_grid_m, (float*)g_state);
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_grid_mass_bwd");
+}
+
+int mpm_density_l1(MpmHandle* h, const void* grid_m, const void* target, double weight, double* loss,
+                   void* g_grid_m, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_density_l1: NULL handle");
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, grid_m, "grid_m"));
+  MPM_TRY(check_aligned(h, target, "target"));
+  MPM_TRY(check_aligned(h, loss, "loss"));
+  MPM_TRY(check_aligned(h, g_grid_m, "g_grid_m", true));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e = h->p.precision == MPM_PREC_FP64
+                      ? mpm::launch_density_l1<double>(L, (const double*)grid_m, (const double*)target, weight, loss,
+                                                       (double*)g_grid_m)
+                      : mpm::launch_density_l1<float>(L, (const float*)grid_m, (const float*)target, weight, loss,
+                                                      (float*)g_grid_m);
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_density_l1");
+}
+
+int mpm_soft_contact(MpmHandle* h, const void* state, const double* pose, double* sums, double* min_dist,
+                     void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_soft_contact: NULL handle");
+  if (h->n_tools == 0) return MPM_OK;
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, state, "state"));
+  MPM_TRY(check_aligned(h, pose, "pose"));
+  MPM_TRY(check_aligned(h, sums, "sums"));
+  MPM_TRY(check_aligned(h, min_dist, "min_dist"));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e =
+      h->p.precision == MPM_PREC_FP64
+          ? mpm::launch_soft_contact<double>(L, h->n_tools, (const double*)state, pose, sums, min_dist)
+          : mpm::launch_soft_contact<float>(L, h->n_tools, (const float*)state, pose, sums, min_dist);
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_soft_contact");
+}
+
+int mpm_soft_contact_bwd(MpmHandle* h, const void* state, const double* pose, const double* sums,
+                         const double* g_min_dist, void* g_state, double* g_pose, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_soft_contact_bwd: NULL handle");
+  if (h->n_tools == 0) return MPM_OK;
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, state, "state"));
+  MPM_TRY(check_aligned(h, pose, "pose"));
+  MPM_TRY(check_aligned(h, sums, "sums"));
+  MPM_TRY(check_aligned(h, g_min_dist, "g_min_dist"));
+  MPM_TRY(check_aligned(h, g_state, "g_state"));
+  MPM_TRY(check_aligned(h, g_pose, "g_pose"));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e = h->p.precision == MPM_PREC_FP64
+                      ? mpm::launch_soft_contact_bwd<double>(L, h->n_tools, (const double*)state, pose, sums,
+                                                             g_min_dist, (double*)g_state, g_pose)
+                      : mpm::launch_soft_contact_bwd<float>(L, h->n_tools, (const float*)state, pose, sums,
+                                                            g_min_dist, (float*)g_state, g_pose);
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_soft_contact_bwd");
+}
+
+int mpm_status(MpmHandle* h, uint32_t* status, int32_t clear, void* stream) {
+  if (!h || !status) return fail(h, MPM_E_INVALID, "mpm_status: NULL argument");
+  MPM_TRY(check_device(h));
+  unsigned int v = 0;
+  cudaError_t e = cudaMemcpyAsync(&v, h->d_status, sizeof(v), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e == cudaSuccess && clear) e = cudaMemsetAsync(h->d_status, 0, sizeof(unsigned int), (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(h, e, "mpm_status");
+  *status = v;
+  return MPM_OK;
+}
+
+int mpm_last_error(MpmHandle* h, char* buf, size_t len) {
+  if (!buf || len == 0) return MPM_E_INVALID;
+  std::string msg;
+  if (h) {
+    msg = h->err;
+  } else {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    msg = g_create_err;
+  }
+  std::snprintf(buf, len, "%s", msg.c_str());
+  return MPM_OK;
+}
+
+int64_t mpm_launch_count(MpmHandle* h) { return h ? h->launches : 0; }
+
+}  // extern "C"

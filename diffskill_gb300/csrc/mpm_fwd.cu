@@ -1,0 +1,155 @@
+// Forward launchers: substep (p2g -> grid_op -> g2p), density grid, density
+// L1 loss and the soft tool-contact distance, for the three precision modes.
+#include "mpm_kernels.cuh"
+#include "mpm_launch.h"
+
+namespace mpm {
+
+template <typename T>
+Consts<T> make_consts(const LaunchCtx& L) {
+  const MpmParams& p = *L.p;
+  Consts<T> c;
+  c.n_grid = p.n_grid;
+  c.n_scenes = p.n_scenes;
+  c.n_particles = p.n_particles;
+  c.ld = p.ld;
+  c.G = L.G;
+  c.dx = T(p.dx);
+  c.inv_dx = T(p.inv_dx);
+  c.dt = T(p.dt);
+  c.p_mass = T(p.p_mass);
+  c.p_vol = T(p.p_vol);
+  c.mu = T(p.mu);
+  c.lam = T(p.lam);
+  c.yield_stress = T(p.yield_stress);
+  c.ks = T(-p.dt * p.p_vol * 4 * p.inv_dx * p.inv_dx);
+  for (int k = 0; k < 3; ++k) c.gdt[k] = T(p.dt * p.gravity[k] * 30);
+  c.ground_friction = T(p.ground_friction);
+  c.x_lo = T(p.lower_bound * p.dx);
+  c.x_hi = T(1.0 - 3 * p.dx);
+  c.status = L.status;
+  return c;
+}
+template Consts<float> make_consts<float>(const LaunchCtx&);
+template Consts<double> make_consts<double>(const LaunchCtx&);
+
+static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+template <typename T, typename S>
+cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const double* pose_f,
+                               const double* pose_f1) {
+  Consts<T> c = make_consts<T>(L);
+  const int64_t nodes = (int64_t)c.n_scenes * c.G;
+  Node<T>* gin = (Node<T>*)L.grid_a;
+  Node<T>* gout = (Node<T>*)L.grid_b;
+  cudaError_t e = cudaMemsetAsync(gin, 0, nodes * sizeof(Node<T>), L.stream);
+  if (e != cudaSuccess) return e;
+  if (c.n_particles > 0) {
+    k_p2g<T, S><<<blocks_for(c.n_particles, 128), 128, 0, L.stream>>>(c, st0, st1, L.pscene, gin);
+    ++*L.launches;
+  }
+  k_grid_op<T><<<(unsigned)(nodes / 128), 128, 0, L.stream>>>(c, gin, gout, L.tools, L.tool_off, pose_f, pose_f1);
+  ++*L.launches;
+  if (c.n_particles > 0) {
+    k_g2p<T><<<blocks_for(c.n_particles, 128), 128, 0, L.stream>>>(c, st0, st1, L.pscene, gout);
+    ++*L.launches;
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_grid_mass(const LaunchCtx& L, const T* st, T* gm) {
+  Consts<T> c = make_consts<T>(L);
+  cudaError_t e = cudaMemsetAsync(gm, 0, (int64_t)c.n_scenes * c.G * sizeof(T), L.stream);
+  if (e != cudaSuccess) return e;
+  if (c.n_particles > 0) {
+    k_grid_mass<T><<<blocks_for(c.n_particles, 128), 128, 0, L.stream>>>(c, st, L.pscene, gm);
+    ++*L.launches;
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_grid_mass_bwd(const LaunchCtx& L, const T* st, const T* ggm, T* gst) {
+  Consts<T> c = make_consts<T>(L);
+  if (c.n_particles > 0) {
+    k_grid_mass_adj<T><<<blocks_for(c.n_particles, 128), 128, 0, L.stream>>>(c, st, L.pscene, ggm, gst);
+    ++*L.launches;
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_density_l1(const LaunchCtx& L, const T* gm, const T* tgt, double weight, double* loss, T* ggm) {
+  const int S = L.p->n_scenes;
+  cudaError_t e = cudaMemsetAsync(loss, 0, S * sizeof(double), L.stream);
+  if (e != cudaSuccess) return e;
+  int bps = (int)((L.G + 256 * 8 - 1) / (256 * 8));
+  if (bps < 1) bps = 1;
+  k_density_l1<T><<<(unsigned)(S * bps), 256, 0, L.stream>>>(L.G, gm, tgt, weight, loss, ggm, bps);
+  ++*L.launches;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// soft contact distance (loss.py:143-162)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128) k_contact_sums(Consts<T> c, const T* __restrict__ st,
+                                                      const int* __restrict__ pscene,
+                                                      const MpmToolDesc* __restrict__ tools,
+                                                      const int* __restrict__ tool_off,
+                                                      const double* __restrict__ pose, double* __restrict__ sums) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= c.n_particles) return;
+  int sc = pscene[p];
+  T x[3];
+  load_row(st, c.ld, p, 0, 3, x);
+  for (int t = tool_off[sc]; t < tool_off[sc + 1]; ++t) {
+    if (tools[t].action_dim <= 0) continue;
+    Tool<T> tl;
+    Pose<T> P;
+    to_tool(tools[t], tl);
+    to_pose(pose + 8 * t, P);
+    T sd = tool_sdf(tl, P, x);
+    double d = (T(0) < sd) ? double(sd) : 0.0;
+    double w = 1.0 / (1.0 + d * d * 10000.0);
+    atomicAdd(sums + 2 * t, w);
+    atomicAdd(sums + 2 * t + 1, d * w);
+  }
+}
+__global__ void k_contact_finish(int n_tools, const double* __restrict__ sums, double* __restrict__ min_dist) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n_tools) min_dist[t] = sums[2 * t] > 0 ? sums[2 * t + 1] / sums[2 * t] : 0.0;
+}
+
+template <typename T>
+cudaError_t launch_soft_contact(const LaunchCtx& L, int n_tools, const T* st, const double* pose, double* sums,
+                                double* min_dist) {
+  Consts<T> c = make_consts<T>(L);
+  cudaError_t e = cudaMemsetAsync(sums, 0, 2 * n_tools * sizeof(double), L.stream);
+  if (e != cudaSuccess) return e;
+  if (c.n_particles > 0) {
+    k_contact_sums<T><<<blocks_for(c.n_particles, 128), 128, 0, L.stream>>>(c, st, L.pscene, L.tools, L.tool_off,
+                                                                              pose, sums);
+    ++*L.launches;
+  }
+  k_contact_finish<<<blocks_for(n_tools, 64), 64, 0, L.stream>>>(n_tools, sums, min_dist);
+  ++*L.launches;
+  return cudaGetLastError();
+}
+
+#define MPM_INST_FWD(T, S) \
+  template cudaError_t launch_substep_fwd<T, S>(const LaunchCtx&, const T*, T*, const double*, const double*);
+MPM_INST_FWD(float, float)
+MPM_INST_FWD(float, double)
+MPM_INST_FWD(double, double)
+#define MPM_INST_T(T)                                                                                  \
+  template cudaError_t launch_grid_mass<T>(const LaunchCtx&, const T*, T*);                            \
+  template cudaError_t launch_grid_mass_bwd<T>(const LaunchCtx&, const T*, const T*, T*);              \
+  template cudaError_t launch_density_l1<T>(const LaunchCtx&, const T*, const T*, double, double*, T*); \
+  template cudaError_t launch_soft_contact<T>(const LaunchCtx&, int, const T*, const double*, double*, double*);
+MPM_INST_T(float)
+MPM_INST_T(double)
+
+}  // namespace mpm

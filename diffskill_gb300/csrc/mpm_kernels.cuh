@@ -1,0 +1,863 @@
+// Kernels of the differentiable MLS-MPM substep, templated on
+//   T  : particle state and grid precision (float or double)
+//   TS : precision of F_tmp, the SVD, the von Mises return map, the stress
+//        and their adjoints (float, or double for the FP32_SVD64 mode).
+//
+// Forward  (MPMSimulator.substep, plb/engine/mpm_simulator.py:307-323):
+//   k_p2g      compute_F_tmp + svd + p2g      (122-129, 166-225)
+//   k_grid_op  grid_op + Primitive.collide    (231-262, primive_base.py:96-120)
+//   k_g2p      g2p                            (265-284)
+// Adjoint  (MPMSimulator.substep_grad, 325-345), after recomputing the grid:
+//   k_g2p_adj      g2p.grad            scatter into the grid-velocity adjoint
+//   k_grid_op_adj  grid_op.grad        per node, tool-pose gradients reduced in FP64
+//   k_p2g_adj      p2g.grad + svd_grad + compute_F_tmp.grad (gather)
+//
+// Particle state is component-major: row k of a frame is st[k*ld + p].
+#pragma once
+#include "../../include/mpm_gb300.h"
+#include "mpm_math.cuh"
+#include "mpm_svd.cuh"
+#include "mpm_tools.cuh"
+
+namespace mpm {
+
+// grid node: (mv or v).xyz, m
+template <typename T>
+struct alignas(4 * sizeof(T)) Node {
+  T x, y, z, w;
+};
+
+template <typename T>
+struct Consts {
+  int n_grid;
+  int n_scenes;
+  int64_t n_particles;
+  int64_t ld;
+  int64_t G;  // n_grid^3
+  T dx, inv_dx, dt, p_mass, p_vol;
+  T mu, lam, yield_stress;
+  T ks;      // -dt * p_vol * 4 * inv_dx^2 (mpm_simulator.py:214)
+  T gdt[3];  // dt * gravity * 30 (mpm_simulator.py:235)
+  T ground_friction;
+  T x_lo, x_hi;  // g2p clamp bounds (mpm_simulator.py:283)
+  unsigned int* status;
+};
+
+MPM_DI void atomic_add_node(Node<float>* n, float a, float b, float c, float d) {
+  atomicAdd(reinterpret_cast<float4*>(n), make_float4(a, b, c, d));
+}
+MPM_DI void atomic_add_node(Node<double>* n, double a, double b, double c, double d) {
+  atomicAdd(&n->x, a);
+  atomicAdd(&n->y, b);
+  atomicAdd(&n->z, c);
+  atomicAdd(&n->w, d);
+}
+MPM_DI void atomic_add_node3(Node<float>* n, float a, float b, float c) {
+  atomicAdd(reinterpret_cast<float4*>(n), make_float4(a, b, c, 0.f));
+}
+MPM_DI void atomic_add_node3(Node<double>* n, double a, double b, double c) {
+  atomicAdd(&n->x, a);
+  atomicAdd(&n->y, b);
+  atomicAdd(&n->z, c);
+}
+
+// quadratic B-spline stencil (mpm_simulator.py:201-204); base truncates like
+// ti.cast(int)
+template <typename T>
+struct Stencil {
+  int base[3];
+  T fx[3];
+  T w[3][3];  // w[k][d]
+};
+template <typename T>
+MPM_DI bool make_stencil(const Consts<T>& c, const T* x, Stencil<T>& s) {
+  bool ok = true;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    T t = x[d] * c.inv_dx - T(0.5);
+    s.base[d] = (int)t;
+    T f = x[d] * c.inv_dx - T(s.base[d]);
+    s.fx[d] = f;
+    s.w[0][d] = T(0.5) * (T(1.5) - f) * (T(1.5) - f);
+    s.w[1][d] = T(0.75) - (f - T(1)) * (f - T(1));
+    s.w[2][d] = T(0.5) * (f - T(0.5)) * (f - T(0.5));
+    ok = ok && (t > T(-1)) && s.base[d] >= 0 && s.base[d] + 2 < c.n_grid;
+  }
+  return ok;
+}
+template <typename T>
+MPM_DI T dweight(const Stencil<T>& s, int k, int d) {
+  T f = s.fx[d];
+  return k == 0 ? -(T(1.5) - f) : (k == 1 ? T(-2) * (f - T(1)) : (f - T(0.5)));
+}
+template <typename T>
+MPM_DI int64_t node_of(const Consts<T>& c, const Stencil<T>& s, int ox, int oy, int oz) {
+  return ((int64_t)(s.base[0] + ox) * c.n_grid + (s.base[1] + oy)) * c.n_grid + (s.base[2] + oz);
+}
+
+template <typename T>
+MPM_DI void load_row(const T* __restrict__ st, int64_t ld, int64_t p, int r0, int n, T* out) {
+#pragma unroll
+  for (int k = 0; k < n; ++k) out[k] = st[(int64_t)(r0 + k) * ld + p];
+}
+template <typename T>
+MPM_DI void store_row(T* __restrict__ st, int64_t ld, int64_t p, int r0, int n, const T* in) {
+#pragma unroll
+  for (int k = 0; k < n; ++k) st[(int64_t)(r0 + k) * ld + p] = in[k];
+}
+
+// ---------------------------------------------------------------------------
+// per-particle p2g math: F_tmp, SVD, von Mises, stress (mpm_simulator.py:
+// 122-124, 127-129, 166-182, 205-215) in the precision S
+// ---------------------------------------------------------------------------
+template <typename S>
+struct P2G {
+  S Ftmp[9], U[9], s[3], V[9];
+  S sigc[3], ehat[3], nrm, dg, k, e[3];
+  bool yield;
+  S newF[9], J, R[9];
+};
+template <typename S>
+struct MatConsts {
+  S dt, mu, lam, ys, ks, p_mass;
+};
+template <typename S>
+MPM_DI void p2g_particle(const MatConsts<S>& m, const S* C, const S* F, P2G<S>& P, S* affine) {
+  S IC[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) IC[i] = m.dt * C[i] + ((i % 4 == 0) ? S(1) : S(0));
+  mm(IC, F, P.Ftmp);
+  svd3(P.Ftmp, P.U, P.s, P.V);
+  S eps[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    P.sigc[i] = (S(0.05) < P.s[i]) ? P.s[i] : S(0.05);
+    eps[i] = mlog(P.sigc[i]);
+  }
+  S mean = (eps[0] + eps[1] + eps[2]) / S(3);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) P.ehat[i] = eps[i] - mean;
+  P.nrm = msqrt(dot3(P.ehat, P.ehat) + S(1e-8));
+  P.dg = P.nrm - m.ys / (S(2) * m.mu);
+  P.yield = P.dg > S(0);
+  if (P.yield) {
+    P.k = P.dg / P.nrm;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) P.e[i] = mexp(eps[i] - P.k * P.ehat[i]);
+    S UD[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc) UD[r * 3 + cc] = P.U[r * 3 + cc] * P.e[cc];
+    mmT(UD, P.V, P.newF);
+  } else {
+    P.k = S(0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) P.e[i] = S(1);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) P.newF[i] = P.Ftmp[i];
+  }
+  P.J = det3(P.newF);
+  mmT(P.U, P.V, P.R);
+  S A[9], st[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) A[i] = P.newF[i] - P.R[i];
+  mmT(A, P.newF, st);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    S v = S(2) * m.mu * st[i];
+    if (i % 4 == 0) v += m.lam * P.J * (P.J - S(1));
+    affine[i] = m.ks * v + m.p_mass * C[i];
+  }
+}
+// adjoint; g_C, g_F are written (not accumulated)
+template <typename S>
+MPM_DI void p2g_particle_vjp(const MatConsts<S>& m, const S* C, const S* F, const P2G<S>& P, const S* g_affine,
+                             const S* g_newF_in, S* g_C, S* g_F) {
+  S g_raw[9], A[9], tmp[9], g_newF[9], g_R[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    g_raw[i] = m.ks * g_affine[i];
+    g_C[i] = m.p_mass * g_affine[i];
+    A[i] = P.newF[i] - P.R[i];
+  }
+  mm(g_raw, P.newF, tmp);  // d/dA of tr(g^T A newF^T)
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    g_R[i] = S(-2) * m.mu * tmp[i];
+    g_newF[i] = S(2) * m.mu * tmp[i] + g_newF_in[i];
+  }
+  mTm(g_raw, A, tmp);  // d/dnewF of the right factor
+  S g_J = m.lam * (S(2) * P.J - S(1)) * (g_raw[0] + g_raw[4] + g_raw[8]);
+  S cf[9];
+  cof3(P.newF, cf);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) g_newF[i] += S(2) * m.mu * tmp[i] + g_J * cf[i];
+  S gU[9], gV[9], gs[3] = {S(0), S(0), S(0)}, g_Ftmp[9];
+  mm(g_R, P.V, gU);   // R = U V^T
+  mTm(g_R, P.U, gV);
+  if (P.yield) {
+    S GV[9], GtU[9], UtGV[9];
+    mm(g_newF, P.V, GV);
+    mTm(g_newF, P.U, GtU);
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc) {
+        gU[r * 3 + cc] += GV[r * 3 + cc] * P.e[cc];
+        gV[r * 3 + cc] += GtU[r * 3 + cc] * P.e[cc];
+      }
+    mTm(P.U, GV, UtGV);
+    S g_eps2[3], g_eps[3], g_ehat[3], g_k = S(0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      g_eps2[i] = UtGV[i * 4] * P.e[i];
+      g_eps[i] = g_eps2[i];
+      g_k -= g_eps2[i] * P.ehat[i];
+      g_ehat[i] = -P.k * g_eps2[i];
+    }
+    S g_nrm = -g_k * P.dg / (P.nrm * P.nrm) + g_k / P.nrm;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) g_ehat[i] += g_nrm * P.ehat[i] / P.nrm;
+    S sh = (g_ehat[0] + g_ehat[1] + g_ehat[2]) / S(3);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      g_eps[i] += g_ehat[i] - sh;
+      gs[i] = (S(0.05) < P.s[i]) ? g_eps[i] / P.sigc[i] : S(0);
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) g_Ftmp[i] = S(0);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) g_Ftmp[i] = g_newF[i];
+  }
+  S gA[9];
+  svd3_bwd(P.U, P.s, P.V, gU, gs, gV, gA);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) g_Ftmp[i] += gA[i];
+  mmT(g_Ftmp, F, tmp);  // Ftmp = (I + dt C) F
+#pragma unroll
+  for (int i = 0; i < 9; ++i) g_C[i] += m.dt * tmp[i];
+  S IC[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) IC[i] = m.dt * C[i] + ((i % 4 == 0) ? S(1) : S(0));
+  mTm(IC, g_Ftmp, g_F);
+}
+
+template <typename T, typename S>
+MPM_DI MatConsts<S> mat_consts(const Consts<T>& c) {
+  MatConsts<S> m;
+  m.dt = S(c.dt);
+  m.mu = S(c.mu);
+  m.lam = S(c.lam);
+  m.ys = S(c.yield_stress);
+  m.ks = S(c.ks);
+  m.p_mass = S(c.p_mass);
+  return m;
+}
+
+// ---------------------------------------------------------------------------
+// forward kernels
+// ---------------------------------------------------------------------------
+template <typename T, typename S>
+__global__ void __launch_bounds__(128) k_p2g(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
+                                             const int* __restrict__ pscene, Node<T>* __restrict__ grid) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= c.n_particles) return;
+  T x[3], v[3];
+  S C[9], F[9];
+  load_row(st, c.ld, p, 0, 3, x);
+  load_row(st, c.ld, p, 3, 3, v);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    C[k] = S(st[(int64_t)(6 + k) * c.ld + p]);
+    F[k] = S(st[(int64_t)(15 + k) * c.ld + p]);
+  }
+  Stencil<T> s;
+  bool ok = make_stencil(c, x, s);
+  MatConsts<S> m = mat_consts<T, S>(c);
+  P2G<S> P;
+  S aff[9];
+  p2g_particle(m, C, F, P, aff);
+  if (st_out) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) st_out[(int64_t)(15 + k) * c.ld + p] = T(P.newF[k]);
+  }
+  if (!ok) {
+    atomicOr(c.status, MPM_STATUS_OUT_OF_GRID);
+    return;
+  }
+  if (!finite(P.J)) atomicOr(c.status, MPM_STATUS_NONFINITE);
+  T affine[9], pm[3];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) affine[k] = T(aff[k]);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) pm[k] = c.p_mass * v[k];
+  Node<T>* g = grid + (int64_t)pscene[p] * c.G;
+#pragma unroll
+  for (int ox = 0; ox < 3; ++ox)
+#pragma unroll
+    for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+      for (int oz = 0; oz < 3; ++oz) {
+        T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
+        T dp[3] = {(T(ox) - s.fx[0]) * c.dx, (T(oy) - s.fx[1]) * c.dx, (T(oz) - s.fx[2]) * c.dx};
+        T mv[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          mv[k] = wgt * (pm[k] + affine[3 * k] * dp[0] + affine[3 * k + 1] * dp[1] + affine[3 * k + 2] * dp[2]);
+        atomic_add_node(g + node_of(c, s, ox, oy, oz), mv[0], mv[1], mv[2], wgt * c.p_mass);
+      }
+}
+
+// Per-CTA tool table of one scene in shared memory.
+template <typename T>
+struct SceneTools {
+  int n;
+  Tool<T> tool[MAX_TOOLS_PER_SCENE];
+  Pose<T> p0[MAX_TOOLS_PER_SCENE], p1[MAX_TOOLS_PER_SCENE];
+};
+template <typename T>
+MPM_DI void to_tool(const MpmToolDesc& d, Tool<T>& t) {
+  t.type = d.type;
+  t.action_dim = d.action_dim;
+  t.friction = T(d.friction);
+  t.softness = T(d.softness);
+  t.radius = T(d.radius);
+  t.cap_h = T(d.cap_h);
+  t.cap_r = T(d.cap_r);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) t.size[k] = T(d.size[k]);
+  t.prism_h[0] = T(d.prism_h[0]);
+  t.prism_h[1] = T(d.prism_h[1]);
+  T pr[4] = {T(d.prot[0]), T(d.prot[1]), T(d.prot[2]), T(d.prot[3])};
+  conj_unit(pr, t.prot_inv);
+}
+template <typename T>
+MPM_DI void to_pose(const double* src, Pose<T>& P) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) P.pos[k] = T(src[k]);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) P.rot[k] = T(src[3 + k]);
+  P.gap = T(src[7]);
+}
+// loads the tools of `scene` (all threads call; one barrier inside)
+template <typename T>
+MPM_DI void load_scene_tools(SceneTools<T>& sh, int scene, const MpmToolDesc* __restrict__ tools,
+                             const int* __restrict__ tool_off, const double* __restrict__ pose_f,
+                             const double* __restrict__ pose_f1) {
+  int t0 = tool_off[scene], t1 = tool_off[scene + 1];
+  int n = t1 - t0;
+  if (threadIdx.x == 0) sh.n = n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    to_tool(tools[t0 + i], sh.tool[i]);
+    to_pose(pose_f + 8 * (t0 + i), sh.p0[i]);
+    to_pose(pose_f1 + 8 * (t0 + i), sh.p1[i]);
+  }
+  __syncthreads();
+}
+
+// wall conditions of grid_op (mpm_simulator.py:241-260) with optional tape
+template <typename T>
+struct WallTape {
+  T v_pre[3][3];
+  bool low[3], up[3];
+};
+template <typename T>
+MPM_DI void walls(const Consts<T>& c, const int* I, T* v, WallTape<T>* tp) {
+  const int bound = 3;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (tp) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) tp->v_pre[d][k] = v[k];
+    }
+    bool low = I[d] < bound && v[d] < T(0);
+    if (tp) tp->low[d] = low;
+    if (low) {
+      if (d != 1 || c.ground_friction == T(0)) {
+        v[d] = T(0);
+      } else if (c.ground_friction < T(10)) {
+        T lin = v[1] + T(1e-30);
+        T vit[3] = {v[0] - T(I[0]) * T(1e-30), v[1] - lin - T(I[1]) * T(1e-30), v[2] - T(I[2]) * T(1e-30)};
+        T lit = msqrt(dot3(vit, vit) + T(1e-8));
+        T a = T(1) + c.ground_friction * lin / lit;
+        T fac = (T(0) < a) ? a : T(0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) v[k] = fac * (vit[k] + T(I[k]) * T(1e-30));
+        v[1] = T(0);
+      } else {
+        v[0] = v[1] = v[2] = T(0);
+      }
+    }
+    bool up = I[d] > c.n_grid - bound && v[d] > T(0);
+    if (tp) tp->up[d] = up;
+    if (up) v[d] = T(0);
+  }
+}
+template <typename T>
+MPM_DI void walls_vjp(const Consts<T>& c, const int* I, const WallTape<T>& tp, T* g) {
+#pragma unroll
+  for (int d = 2; d >= 0; --d) {
+    if (tp.up[d]) g[d] = T(0);
+    if (!tp.low[d]) continue;
+    if (d != 1 || c.ground_friction == T(0)) {
+      g[d] = T(0);
+    } else if (c.ground_friction < T(10)) {
+      const T* v = tp.v_pre[d];
+      T lin = v[1] + T(1e-30);
+      T vit[3] = {v[0] - T(I[0]) * T(1e-30), v[1] - lin - T(I[1]) * T(1e-30), v[2] - T(I[2]) * T(1e-30)};
+      T lit = msqrt(dot3(vit, vit) + T(1e-8));
+      T a = T(1) + c.ground_friction * lin / lit;
+      T fac = (T(0) < a) ? a : T(0);
+      const T go[3] = {g[0], T(0), g[2]};
+      const T w[3] = {vit[0] + T(I[0]) * T(1e-30), vit[1] + T(I[1]) * T(1e-30), vit[2] + T(I[2]) * T(1e-30)};
+      T g_fac = dot3(go, w);
+      T g_vit[3] = {fac * go[0], fac * go[1], fac * go[2]};
+      T g_lin = T(0), g_lit = T(0);
+      if (T(0) < a) {
+        g_lin = g_fac * c.ground_friction / lit;
+        g_lit = -g_fac * c.ground_friction * lin / (lit * lit);
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) g_vit[k] += g_lit * vit[k] / lit;
+      g_lin -= g_vit[1];
+      g[0] = g_vit[0];
+      g[1] = g_vit[1] + g_lin;
+      g[2] = g_vit[2];
+    } else {
+      g[0] = g[1] = g[2] = T(0);
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_grid_op(Consts<T> c, const Node<T>* __restrict__ grid_in,
+                                                 Node<T>* __restrict__ grid_out,
+                                                 const MpmToolDesc* __restrict__ tools,
+                                                 const int* __restrict__ tool_off, const double* __restrict__ pose_f,
+                                                 const double* __restrict__ pose_f1) {
+  __shared__ SceneTools<T> sh;
+  int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // G % blockDim == 0
+  int scene = (int)(((int64_t)blockIdx.x * blockDim.x) / c.G);
+  load_scene_tools(sh, scene, tools, tool_off, pose_f, pose_f1);
+  Node<T> in = grid_in[gid];
+  Node<T> out = {T(0), T(0), T(0), in.w};
+  if (in.w > T(1e-12)) {
+    int64_t id = gid - (int64_t)scene * c.G;
+    int I[3] = {(int)(id / ((int64_t)c.n_grid * c.n_grid)), (int)((id / c.n_grid) % c.n_grid),
+                (int)(id % c.n_grid)};
+    T inv = T(1) / in.w;
+    T v[3] = {inv * in.x + c.gdt[0], inv * in.y + c.gdt[1], inv * in.z + c.gdt[2]};
+    const T p[3] = {T(I[0]) * c.dx, T(I[1]) * c.dx, T(I[2]) * c.dx};
+    for (int t = 0; t < sh.n; ++t) tool_collide(sh.tool[t], sh.p0[t], sh.p1[t], p, c.dt, v);
+    walls(c, I, v, (WallTape<T>*)nullptr);
+    if (!(finite(v[0]) && finite(v[1]) && finite(v[2]))) atomicOr(c.status, MPM_STATUS_NONFINITE);
+    out.x = v[0];
+    out.y = v[1];
+    out.z = v[2];
+  }
+  grid_out[gid] = out;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_g2p(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
+                                             const int* __restrict__ pscene, const Node<T>* __restrict__ grid) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= c.n_particles) return;
+  T x[3];
+  load_row(st, c.ld, p, 0, 3, x);
+  Stencil<T> s;
+  if (!make_stencil(c, x, s)) {  // flagged by k_p2g; the particle keeps its state
+#pragma unroll
+    for (int k = 0; k < 15; ++k) st_out[(int64_t)k * c.ld + p] = st[(int64_t)k * c.ld + p];
+    return;
+  }
+  const Node<T>* g = grid + (int64_t)pscene[p] * c.G;
+  T nv[3] = {T(0), T(0), T(0)}, nC[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) nC[k] = T(0);
+  const T k4 = T(4) * c.inv_dx;
+#pragma unroll
+  for (int ox = 0; ox < 3; ++ox)
+#pragma unroll
+    for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+      for (int oz = 0; oz < 3; ++oz) {
+        T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
+        Node<T> gv = g[node_of(c, s, ox, oy, oz)];
+        const T gvv[3] = {gv.x, gv.y, gv.z};
+        const T dp[3] = {T(ox) - s.fx[0], T(oy) - s.fx[1], T(oz) - s.fx[2]};
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          nv[i] += wgt * gvv[i];
+#pragma unroll
+          for (int j = 0; j < 3; ++j) nC[i * 3 + j] += k4 * wgt * gvv[i] * dp[j];
+        }
+      }
+  T xn[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    T t = x[i] + c.dt * nv[i];
+    T mn = (t < c.x_hi) ? t : c.x_hi;
+    xn[i] = (c.x_lo < mn) ? mn : c.x_lo;
+  }
+  store_row(st_out, c.ld, p, 0, 3, xn);
+  store_row(st_out, c.ld, p, 3, 3, nv);
+  store_row(st_out, c.ld, p, 6, 9, nC);
+}
+
+// ---------------------------------------------------------------------------
+// adjoint kernels
+// ---------------------------------------------------------------------------
+// g2p.grad: writes the x rows of g0 (partial) and scatters into g_grid
+template <typename T>
+__global__ void __launch_bounds__(128) k_g2p_adj(Consts<T> c, const T* __restrict__ st, const T* __restrict__ g1,
+                                                 T* __restrict__ g0, const int* __restrict__ pscene,
+                                                 const Node<T>* __restrict__ grid, Node<T>* __restrict__ g_grid) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= c.n_particles) return;
+  T x[3];
+  load_row(st, c.ld, p, 0, 3, x);
+  Stencil<T> s;
+  if (!make_stencil(c, x, s)) {
+    const T z[3] = {T(0), T(0), T(0)};
+    store_row(g0, c.ld, p, 0, 3, z);
+    return;
+  }
+  const int64_t off = (int64_t)pscene[p] * c.G;
+  const Node<T>* g = grid + off;
+  Node<T>* gg = g_grid + off;
+  T nv[3] = {T(0), T(0), T(0)};
+#pragma unroll
+  for (int ox = 0; ox < 3; ++ox)
+#pragma unroll
+    for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+      for (int oz = 0; oz < 3; ++oz) {
+        T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
+        Node<T> n = g[node_of(c, s, ox, oy, oz)];
+        nv[0] += wgt * n.x;
+        nv[1] += wgt * n.y;
+        nv[2] += wgt * n.z;
+      }
+  T gx1[3], gnv[3], gC[9], gx[3];
+  load_row(g1, c.ld, p, 0, 3, gx1);
+  load_row(g1, c.ld, p, 3, 3, gnv);
+  load_row(g1, c.ld, p, 6, 9, gC);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    T t = x[i] + c.dt * nv[i];
+    T mn = (t < c.x_hi) ? t : c.x_hi;
+    bool pass = (t < c.x_hi) && (c.x_lo < mn);
+    T gt = pass ? gx1[i] : T(0);
+    gx[i] = gt;
+    gnv[i] += c.dt * gt;
+  }
+  const T k4 = T(4) * c.inv_dx;
+  T gw[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) gw[a][b] = T(0);
+  T gfx[3] = {T(0), T(0), T(0)};
+#pragma unroll
+  for (int ox = 0; ox < 3; ++ox)
+#pragma unroll
+    for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+      for (int oz = 0; oz < 3; ++oz) {
+        T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
+        const T dp[3] = {T(ox) - s.fx[0], T(oy) - s.fx[1], T(oz) - s.fx[2]};
+        Node<T> n = g[node_of(c, s, ox, oy, oz)];
+        const T gv[3] = {n.x, n.y, n.z};
+        T gCd[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) gCd[i] = gC[3 * i] * dp[0] + gC[3 * i + 1] * dp[1] + gC[3 * i + 2] * dp[2];
+        atomic_add_node3(gg + node_of(c, s, ox, oy, oz), wgt * (gnv[0] + k4 * gCd[0]), wgt * (gnv[1] + k4 * gCd[1]),
+                         wgt * (gnv[2] + k4 * gCd[2]));
+        T g_wgt = dot3(gv, gnv) + k4 * dot3(gv, gCd);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) gfx[j] -= k4 * wgt * (gC[j] * gv[0] + gC[3 + j] * gv[1] + gC[6 + j] * gv[2]);
+        gw[ox][0] += g_wgt * s.w[oy][1] * s.w[oz][2];
+        gw[oy][1] += g_wgt * s.w[ox][0] * s.w[oz][2];
+        gw[oz][2] += g_wgt * s.w[ox][0] * s.w[oy][1];
+      }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) gfx[d] += gw[k][d] * dweight(s, k, d);
+    gx[d] += c.inv_dx * gfx[d];
+  }
+  store_row(g0, c.ld, p, 0, 3, gx);
+}
+
+// FP64 warp reduction of one value; lane 0 adds into shared accumulator
+MPM_DI void warp_add_to(double* acc, double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(acc, v);
+}
+
+// grid_op.grad: g_grid (velocity adjoint, xyz) -> g_in (mv.xyz, m); tool
+// pose gradients of frames f and f+1 reduced in FP64.
+template <typename T>
+__global__ void __launch_bounds__(128) k_grid_op_adj(Consts<T> c, const Node<T>* __restrict__ grid_in,
+                                                     const Node<T>* __restrict__ g_grid,
+                                                     Node<T>* __restrict__ g_in,
+                                                     const MpmToolDesc* __restrict__ tools,
+                                                     const int* __restrict__ tool_off,
+                                                     const double* __restrict__ pose_f,
+                                                     const double* __restrict__ pose_f1, double* __restrict__ g_pose_f,
+                                                     double* __restrict__ g_pose_f1) {
+  __shared__ SceneTools<T> sh;
+  __shared__ double acc[MAX_TOOLS_PER_SCENE][16];
+  int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int scene = (int)(((int64_t)blockIdx.x * blockDim.x) / c.G);
+  for (int i = threadIdx.x; i < MAX_TOOLS_PER_SCENE * 16; i += blockDim.x) (&acc[0][0])[i] = 0.0;
+  load_scene_tools(sh, scene, tools, tool_off, pose_f, pose_f1);
+  Node<T> in = grid_in[gid];
+  Node<T> go = g_grid[gid];
+  bool active = in.w > T(1e-12) && (go.x != T(0) || go.y != T(0) || go.z != T(0));
+  Node<T> res = {T(0), T(0), T(0), T(0)};
+  int64_t id = gid - (int64_t)scene * c.G;
+  int I[3] = {(int)(id / ((int64_t)c.n_grid * c.n_grid)), (int)((id / c.n_grid) % c.n_grid), (int)(id % c.n_grid)};
+  const T p[3] = {T(I[0]) * c.dx, T(I[1]) * c.dx, T(I[2]) * c.dx};
+  T vt[MAX_TOOLS_PER_SCENE + 1][3];
+  WallTape<T> wt;
+  T g[3] = {go.x, go.y, go.z};
+  T inv = T(1) / in.w;
+  if (active) {
+    T v[3] = {inv * in.x + c.gdt[0], inv * in.y + c.gdt[1], inv * in.z + c.gdt[2]};
+    for (int t = 0; t < sh.n; ++t) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) vt[t][k] = v[k];
+      tool_collide(sh.tool[t], sh.p0[t], sh.p1[t], p, c.dt, v);
+    }
+    walls(c, I, v, &wt);
+    walls_vjp(c, I, wt, g);
+  }
+  const int nt = sh.n;
+  for (int t = nt - 1; t >= 0; --t) {
+    PoseGrad<T> g0, g1;
+    g0.zero();
+    g1.zero();
+    if (active) tool_collide_vjp(sh.tool[t], sh.p0[t], sh.p1[t], p, c.dt, vt[t], g, g0, g1);
+    const bool any = __any_sync(0xffffffffu, active);
+    if (any) {
+      warp_add_to(&acc[t][0], double(g0.pos[0]));
+      warp_add_to(&acc[t][1], double(g0.pos[1]));
+      warp_add_to(&acc[t][2], double(g0.pos[2]));
+      warp_add_to(&acc[t][3], double(g0.rot[0]));
+      warp_add_to(&acc[t][4], double(g0.rot[1]));
+      warp_add_to(&acc[t][5], double(g0.rot[2]));
+      warp_add_to(&acc[t][6], double(g0.rot[3]));
+      warp_add_to(&acc[t][7], double(g0.gap));
+      warp_add_to(&acc[t][8], double(g1.pos[0]));
+      warp_add_to(&acc[t][9], double(g1.pos[1]));
+      warp_add_to(&acc[t][10], double(g1.pos[2]));
+      warp_add_to(&acc[t][11], double(g1.rot[0]));
+      warp_add_to(&acc[t][12], double(g1.rot[1]));
+      warp_add_to(&acc[t][13], double(g1.rot[2]));
+      warp_add_to(&acc[t][14], double(g1.rot[3]));
+      warp_add_to(&acc[t][15], double(g1.gap));
+    }
+  }
+  if (active) {
+    res.x = g[0] * inv;
+    res.y = g[1] * inv;
+    res.z = g[2] * inv;
+    res.w = -(g[0] * in.x + g[1] * in.y + g[2] * in.z) * inv * inv;
+  }
+  g_in[gid] = res;
+  __syncthreads();
+  int t0 = tool_off[scene];
+  for (int i = threadIdx.x; i < nt * 16; i += blockDim.x) {
+    int t = i / 16, k = i % 16;
+    double v = acc[t][k];
+    if (v != 0.0) {
+      double* dst = (k < 8) ? (g_pose_f + 8 * (t0 + t) + k) : (g_pose_f1 + 8 * (t0 + t) + (k - 8));
+      atomicAdd(dst, v);
+    }
+  }
+}
+
+// p2g.grad + svd_grad + compute_F_tmp.grad: gathers g_in; reads the partial
+// x gradient left in g0 by k_g2p_adj and writes all 24 rows of g0.
+template <typename T, typename S>
+__global__ void __launch_bounds__(128) k_p2g_adj(Consts<T> c, const T* __restrict__ st, const T* __restrict__ g1,
+                                                 T* __restrict__ g0, const int* __restrict__ pscene,
+                                                 const Node<T>* __restrict__ g_in) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= c.n_particles) return;
+  T x[3], v[3];
+  S C[9], F[9];
+  load_row(st, c.ld, p, 0, 3, x);
+  load_row(st, c.ld, p, 3, 3, v);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    C[k] = S(st[(int64_t)(6 + k) * c.ld + p]);
+    F[k] = S(st[(int64_t)(15 + k) * c.ld + p]);
+  }
+  Stencil<T> s;
+  bool ok = make_stencil(c, x, s);
+  MatConsts<S> m = mat_consts<T, S>(c);
+  P2G<S> P;
+  S aff[9];
+  p2g_particle(m, C, F, P, aff);
+  T affine[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) affine[k] = T(aff[k]);
+  T gx[3], gv[3] = {T(0), T(0), T(0)};
+  load_row(g0, c.ld, p, 0, 3, gx);
+  S g_aff[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) g_aff[k] = S(0);
+  if (ok) {
+    const Node<T>* gg = g_in + (int64_t)pscene[p] * c.G;
+    T ga[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) ga[k] = T(0);
+    T gw[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) gw[a][b] = T(0);
+    T gfx[3] = {T(0), T(0), T(0)};
+#pragma unroll
+    for (int ox = 0; ox < 3; ++ox)
+#pragma unroll
+      for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+        for (int oz = 0; oz < 3; ++oz) {
+          T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
+          const T dp[3] = {(T(ox) - s.fx[0]) * c.dx, (T(oy) - s.fx[1]) * c.dx, (T(oz) - s.fx[2]) * c.dx};
+          Node<T> n = gg[node_of(c, s, ox, oy, oz)];
+          const T gn[3] = {n.x, n.y, n.z};
+          T contrib[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k)
+            contrib[k] = c.p_mass * v[k] + affine[3 * k] * dp[0] + affine[3 * k + 1] * dp[1] + affine[3 * k + 2] * dp[2];
+          T g_wgt = dot3(gn, contrib) + n.w * c.p_mass;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            gv[k] += wgt * c.p_mass * gn[k];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) ga[3 * k + j] += wgt * gn[k] * dp[j];
+          }
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+            gfx[j] -= c.dx * wgt * (affine[j] * gn[0] + affine[3 + j] * gn[1] + affine[6 + j] * gn[2]);
+          gw[ox][0] += g_wgt * s.w[oy][1] * s.w[oz][2];
+          gw[oy][1] += g_wgt * s.w[ox][0] * s.w[oz][2];
+          gw[oz][2] += g_wgt * s.w[ox][0] * s.w[oy][1];
+        }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) gfx[d] += gw[k][d] * dweight(s, k, d);
+      gx[d] += c.inv_dx * gfx[d];
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) g_aff[k] = S(ga[k]);
+  }
+  S gF1[9], gC[9], gF[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) gF1[k] = S(g1[(int64_t)(15 + k) * c.ld + p]);
+  p2g_particle_vjp(m, C, F, P, g_aff, gF1, gC, gF);
+  store_row(g0, c.ld, p, 0, 3, gx);
+  store_row(g0, c.ld, p, 3, 3, gv);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    g0[(int64_t)(6 + k) * c.ld + p] = T(gC[k]);
+    g0[(int64_t)(15 + k) * c.ld + p] = T(gF[k]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// density grid and losses
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128) k_grid_mass(Consts<T> c, const T* __restrict__ st,
+                                                   const int* __restrict__ pscene, T* __restrict__ gm) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= c.n_particles) return;
+  T x[3];
+  load_row(st, c.ld, p, 0, 3, x);
+  Stencil<T> s;
+  if (!make_stencil(c, x, s)) {
+    atomicOr(c.status, MPM_STATUS_OUT_OF_GRID);
+    return;
+  }
+  T* g = gm + (int64_t)pscene[p] * c.G;
+#pragma unroll
+  for (int ox = 0; ox < 3; ++ox)
+#pragma unroll
+    for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+      for (int oz = 0; oz < 3; ++oz)
+        atomicAdd(g + node_of(c, s, ox, oy, oz), s.w[ox][0] * s.w[oy][1] * s.w[oz][2] * c.p_mass);
+}
+template <typename T>
+__global__ void __launch_bounds__(128) k_grid_mass_adj(Consts<T> c, const T* __restrict__ st,
+                                                       const int* __restrict__ pscene, const T* __restrict__ ggm,
+                                                       T* __restrict__ gst) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= c.n_particles) return;
+  T x[3];
+  load_row(st, c.ld, p, 0, 3, x);
+  Stencil<T> s;
+  if (!make_stencil(c, x, s)) return;
+  const T* g = ggm + (int64_t)pscene[p] * c.G;
+  T gw[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) gw[a][b] = T(0);
+#pragma unroll
+  for (int ox = 0; ox < 3; ++ox)
+#pragma unroll
+    for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+      for (int oz = 0; oz < 3; ++oz) {
+        T gg = g[node_of(c, s, ox, oy, oz)] * c.p_mass;
+        gw[ox][0] += gg * s.w[oy][1] * s.w[oz][2];
+        gw[oy][1] += gg * s.w[ox][0] * s.w[oz][2];
+        gw[oz][2] += gg * s.w[ox][0] * s.w[oy][1];
+      }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    T gfx = T(0);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) gfx += gw[k][d] * dweight(s, k, d);
+    gst[(int64_t)d * c.ld + p] += c.inv_dx * gfx;
+  }
+}
+// per-scene sum |m - target| in FP64; blocks never straddle scenes
+template <typename T>
+__global__ void __launch_bounds__(256) k_density_l1(int64_t G, const T* __restrict__ gm, const T* __restrict__ tgt,
+                                                    double weight, double* __restrict__ loss, T* __restrict__ ggm,
+                                                    int blocks_per_scene) {
+  int scene = blockIdx.x / blocks_per_scene;
+  int b = blockIdx.x % blocks_per_scene;
+  const T* a = gm + (int64_t)scene * G;
+  const T* t = tgt + (int64_t)scene * G;
+  double acc = 0.0;
+  for (int64_t i = (int64_t)b * blockDim.x + threadIdx.x; i < G; i += (int64_t)blocks_per_scene * blockDim.x) {
+    T d = a[i] - t[i];
+    acc += fabs(double(d));
+    if (ggm) ggm[(int64_t)scene * G + i] = T(weight) * sgn(d);
+  }
+  __shared__ double red[8];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    atomicAdd(loss + scene, weight * s);
+  }
+}
+
+}  // namespace mpm

@@ -1,0 +1,347 @@
+"""Host runtime of the GB300 MPM substep.
+
+``MpmEngine`` owns one C-ABI handle (include/mpm_gb300.h) for a batch of
+independent scenes that share the grid resolution, time step and material.
+State lives in torch CUDA tensors owned here; the library only receives raw
+pointers and the current stream.
+
+``Horizon`` runs a whole action sequence: forward with a checkpoint every
+``k`` substeps, then the reverse sweep that recomputes each k-substep segment
+from its checkpoint and applies the hand-written adjoint substep by substep.
+This replaces the reference's store-every-frame fields (x, v, C, F of shape
+``(max_steps, N)``, plb/engine/mpm_simulator.py:38-43) and its per-substep
+``substep_grad`` (325-345), so long horizons fit in HBM.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+from .config import (PREC_FP64, TOOL_GRIPPER, PrimitiveConfig, SimulatorConfig, action_dims)
+
+N_ROWS = 24  # x(3) v(3) C(9) F(9)
+
+
+def _ptr(t: Optional[torch.Tensor]):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream() -> ctypes.c_void_p:
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class MpmEngine:
+    """Batched scenes on one GPU behind one library handle."""
+
+    def __init__(self, sim: SimulatorConfig, tools_per_scene: Sequence[Sequence[PrimitiveConfig]],
+                 n_per_scene: Sequence[int], softness: float = 666.0, device: Optional[torch.device] = None):
+        if not torch.cuda.is_available():
+            raise _lib.MpmError("diffskill_gb300 needs a CUDA device; there is no CPU path")
+        self.lib = _lib.load()
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.sim = sim
+        self.prec = sim.precision_code
+        self.dtype = torch.float64 if self.prec == PREC_FP64 else torch.float32
+        self.S = len(n_per_scene)
+        if len(tools_per_scene) != self.S:
+            raise ValueError("tools_per_scene and n_per_scene must have one entry per scene")
+        self.n_per_scene = [int(n) for n in n_per_scene]
+        self.offsets = np.concatenate([[0], np.cumsum(self.n_per_scene)]).astype(np.int64)
+        self.P = int(self.offsets[-1])
+        self.ld = max(32, -(-self.P // 32) * 32)
+        self.n_grid = sim.grid
+        self.G = self.n_grid ** 3
+        self.n_sub = sim.n_substeps
+        self.softness = float(softness)
+
+        p = _lib.MpmParams()
+        p.abi_version = _lib.ABI_VERSION
+        p.precision = self.prec
+        p.n_grid = self.n_grid
+        p.n_scenes = self.S
+        p.n_particles = self.P
+        p.ld = self.ld
+        p.dx, p.inv_dx, p.dt, p.p_vol, p.p_mass = sim.dx, sim.inv_dx, sim.step_dt, sim.p_vol, sim.p_mass
+        p.mu, p.lam, p.yield_stress = sim.mu, sim.lam, sim.yield_stress
+        p.gravity[:] = [float(g) for g in sim.gravity]
+        p.ground_friction = sim.ground_friction
+        p.lower_bound = sim.lower_bound
+        self.params = p
+        offs = (ctypes.c_int64 * (self.S + 1))(*[int(o) for o in self.offsets])
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.mpm_create(ctypes.byref(p), offs, ctypes.byref(h)), None, "mpm_create")
+        self.h = h
+
+        # tools, sorted by scene
+        self.tool_cfgs: List[PrimitiveConfig] = []
+        self.tool_scene: List[int] = []
+        self.scene_tools: List[List[int]] = []
+        for s, tl in enumerate(tools_per_scene):
+            idx = []
+            for t in tl:
+                idx.append(len(self.tool_cfgs))
+                self.tool_cfgs.append(t)
+                self.tool_scene.append(s)
+            self.scene_tools.append(idx)
+        self.T = len(self.tool_cfgs)
+        descs = (_lib.MpmToolDesc * max(self.T, 1))()
+        for i, (t, s) in enumerate(zip(self.tool_cfgs, self.tool_scene)):
+            d = descs[i]
+            d.type = t.type_code
+            d.action_dim = int(t.action.dim)
+            d.scene = s
+            d.friction, d.softness = t.friction, self.softness
+            d.radius, d.cap_h, d.cap_r = t.radius, t.h, t.r
+            d.size[:] = list(t.size)
+            d.prism_h[:] = list(t.prism_h)
+            d.prot[:] = list(t.prot)
+            d.min_gap, d.max_gap = t.minimal_gap, t.maximal_gap
+            d.lower[:] = list(t.lower_bound)
+            d.upper[:] = list(t.upper_bound)
+            d.action_scale[:] = list(t.scale7())
+        self._descs = descs
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.mpm_set_tools(self.h, descs, self.T), self.h, "mpm_set_tools")
+        self.scene_action_dims = [action_dims([self.tool_cfgs[i] for i in idx]) for idx in self.scene_tools]
+        self.pose0 = torch.tensor([list(t.init_state) for t in self.tool_cfgs] or np.zeros((0, 8)),
+                                  dtype=torch.float64, device=self.device).reshape(self.T, 8)
+        self.ds = torch.empty(max(2 * self.T, 2), dtype=torch.float64, device=self.device)  # contact sums
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and self.lib is not None:
+            try:
+                self.lib.mpm_destroy(h)
+            except Exception:
+                pass
+            self.h = None
+
+    # ------------------------------------------------------------------ state
+    def new_state(self) -> torch.Tensor:
+        return torch.zeros((N_ROWS, self.ld), dtype=self.dtype, device=self.device)
+
+    def init_state(self, xs: Sequence[np.ndarray]) -> torch.Tensor:
+        """``reset_kernel`` (mpm_simulator.py:402-409): x given, v=0, F=I, C=0."""
+        st = self.new_state()
+        x = np.concatenate([np.asarray(a, dtype=np.float64).reshape(-1, 3) for a in xs])
+        if x.shape[0] != self.P:
+            raise ValueError(f"expected {self.P} particles, got {x.shape[0]}")
+        st[0:3, :self.P] = torch.as_tensor(x.T, dtype=self.dtype, device=self.device)
+        st[15, :] = 1
+        st[19, :] = 1
+        st[23, :] = 1
+        return st
+
+    def expand_actions(self, actions_per_scene: Sequence[np.ndarray] | torch.Tensor) -> torch.Tensor:
+        """[A, action_dim_s] per scene (reference flat layout) -> [A, T, 8], clipped to [-1, 1]."""
+        if isinstance(actions_per_scene, torch.Tensor) and actions_per_scene.dim() == 3 \
+                and actions_per_scene.shape[1:] == (self.T, 8):
+            return actions_per_scene.to(torch.float64).clamp(-1, 1).contiguous()
+        A = int(np.asarray(actions_per_scene[0]).shape[0]) if self.S else 0
+        out = torch.zeros((A, self.T, 8), dtype=torch.float64, device=self.device)
+        for s, idx in enumerate(self.scene_tools):
+            a = torch.as_tensor(np.asarray(actions_per_scene[s], dtype=np.float64), device=self.device).reshape(A, -1)
+            a = a.clamp(-1, 1)
+            dims = self.scene_action_dims[s]
+            for j, t in enumerate(idx):
+                d = dims[j + 1] - dims[j]
+                out[:, t, :d] = a[:, dims[j]:dims[j + 1]]
+        return out
+
+    def collapse_action_grad(self, g: torch.Tensor) -> List[torch.Tensor]:
+        """[A, T, 8] -> per scene [A, action_dim_s] (reference flat layout)."""
+        out = []
+        for s, idx in enumerate(self.scene_tools):
+            dims = self.scene_action_dims[s]
+            parts = [g[:, t, :dims[j + 1] - dims[j]] for j, t in enumerate(idx)]
+            out.append(torch.cat(parts, dim=1) if parts else g.new_zeros((g.shape[0], 0)))
+        return out
+
+    # -------------------------------------------------------------- C calls
+    def tools_action(self, action: torch.Tensor, vel: torch.Tensor, pose: torch.Tensor) -> None:
+        _lib.check(self.lib.mpm_tools_action(self.h, _ptr(action), _ptr(vel), _ptr(pose), self.n_sub, _stream()),
+                   self.h, "mpm_tools_action")
+
+    def tools_action_bwd(self, vel, pose, g_pose, g_action) -> None:
+        _lib.check(self.lib.mpm_tools_action_bwd(self.h, _ptr(vel), _ptr(pose), _ptr(g_pose), _ptr(g_action),
+                                                 self.n_sub, _stream()), self.h, "mpm_tools_action_bwd")
+
+    def substep(self, st0, st1, pose_f, pose_f1) -> None:
+        _lib.check(self.lib.mpm_substep_fwd(self.h, _ptr(st0), _ptr(st1), _ptr(pose_f), _ptr(pose_f1), _stream()),
+                   self.h, "mpm_substep_fwd")
+
+    def substep_bwd(self, st0, g1, g0, pose_f, pose_f1, gp_f, gp_f1) -> None:
+        _lib.check(self.lib.mpm_substep_bwd(self.h, _ptr(st0), _ptr(g1), _ptr(g0), _ptr(pose_f), _ptr(pose_f1),
+                                            _ptr(gp_f), _ptr(gp_f1), _stream()), self.h, "mpm_substep_bwd")
+
+    def grid_mass(self, st: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        if out is None:
+            out = torch.empty((self.S, self.G), dtype=self.dtype, device=self.device)
+        _lib.check(self.lib.mpm_grid_mass(self.h, _ptr(st), _ptr(out), _stream()), self.h, "mpm_grid_mass")
+        return out
+
+    def grid_mass_bwd(self, st, g_gm, g_st) -> None:
+        _lib.check(self.lib.mpm_grid_mass_bwd(self.h, _ptr(st), _ptr(g_gm), _ptr(g_st), _stream()), self.h,
+                   "mpm_grid_mass_bwd")
+
+    def density_l1(self, gm, target, weight: float = 1.0, g_gm=None) -> torch.Tensor:
+        loss = torch.empty(self.S, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.mpm_density_l1(self.h, _ptr(gm), _ptr(target), float(weight), _ptr(loss), _ptr(g_gm),
+                                           _stream()), self.h, "mpm_density_l1")
+        return loss
+
+    def soft_contact(self, st, pose) -> tuple:
+        md = torch.empty(max(self.T, 1), dtype=torch.float64, device=self.device)
+        sums = torch.empty((max(self.T, 1), 2), dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.mpm_soft_contact(self.h, _ptr(st), _ptr(pose), _ptr(sums), _ptr(md), _stream()),
+                   self.h, "mpm_soft_contact")
+        return md[:self.T], sums
+
+    def soft_contact_bwd(self, st, pose, sums, g_md, g_st, g_pose) -> None:
+        _lib.check(self.lib.mpm_soft_contact_bwd(self.h, _ptr(st), _ptr(pose), _ptr(sums), _ptr(g_md), _ptr(g_st),
+                                                 _ptr(g_pose), _stream()), self.h, "mpm_soft_contact_bwd")
+
+    def status(self, clear: bool = True) -> int:
+        v = ctypes.c_uint32(0)
+        _lib.check(self.lib.mpm_status(self.h, ctypes.byref(v), int(clear), _stream()), self.h, "mpm_status")
+        return int(v.value)
+
+    def check_status(self) -> None:
+        st = self.status(clear=True)
+        if st & _lib.STATUS_NONFINITE:
+            raise FloatingPointError("MPM substep produced a NaN/Inf (device status word)")
+        if st & _lib.STATUS_OUT_OF_GRID:
+            raise _lib.MpmError("a particle stencil left the grid; its scatter was skipped")
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.mpm_launch_count(self.h))
+
+    # ------------------------------------------------------------- helpers
+    def targets(self, grids: Sequence[np.ndarray]) -> torch.Tensor:
+        return torch.as_tensor(np.stack([np.asarray(g, dtype=np.float64).reshape(-1) for g in grids]),
+                               dtype=self.dtype, device=self.device).contiguous()
+
+    def scene_slice(self, s: int) -> slice:
+        return slice(int(self.offsets[s]), int(self.offsets[s + 1]))
+
+
+class Horizon:
+    """Device buffers and the forward/backward sweep over ``n_actions`` actions.
+
+    ``ckpt_every`` = k: the state is kept every k substeps (k=1 keeps every
+    frame, as the reference does); the backward pass recomputes each segment
+    of k substeps from its checkpoint before running its adjoint.
+    """
+
+    def __init__(self, eng: MpmEngine, n_actions: int, ckpt_every: int = 10):
+        self.eng = eng
+        self.A = int(n_actions)
+        self.F = self.A * eng.n_sub
+        k = int(ckpt_every) if ckpt_every else eng.n_sub
+        if self.F % k != 0:
+            raise ValueError(f"checkpoint interval {k} must divide the horizon of {self.F} substeps")
+        self.k = k
+        dev, dt = eng.device, eng.dtype
+        self.n_ckpt = self.F // k + 1
+        self.ckpt = torch.zeros((self.n_ckpt, N_ROWS, eng.ld), dtype=dt, device=dev)
+        self.seg = torch.zeros((max(k, 2), N_ROWS, eng.ld), dtype=dt, device=dev)
+        T = max(eng.T, 1)
+        self.pose = torch.zeros((self.F + 1, T, 8), dtype=torch.float64, device=dev)
+        self.vel = torch.zeros((self.F, T, 8), dtype=torch.float64, device=dev)
+        self.acts = torch.zeros((self.A, T, 8), dtype=torch.float64, device=dev)
+        self.g_pose = torch.zeros_like(self.pose)
+        self.g_act = torch.zeros_like(self.acts)
+        self.g = torch.zeros((2, N_ROWS, eng.ld), dtype=dt, device=dev)
+        self.gm = torch.zeros((eng.S, eng.G), dtype=dt, device=dev)
+        self.g_gm = torch.zeros_like(self.gm)
+
+    def bytes(self) -> int:
+        return sum(t.numel() * t.element_size() for t in
+                   (self.ckpt, self.seg, self.pose, self.vel, self.g, self.gm, self.g_gm, self.g_pose))
+
+    @property
+    def final(self) -> torch.Tensor:
+        return self.ckpt[self.n_ckpt - 1]
+
+    def forward(self, state0: torch.Tensor, actions: torch.Tensor, pose0: Optional[torch.Tensor] = None) -> None:
+        """Run all actions: ``GradModel.forward_step`` for each action (function.py:166-175)."""
+        eng, n = self.eng, self.eng.n_sub
+        self.ckpt[0].copy_(state0)
+        if eng.T:
+            self.pose[0].copy_(eng.pose0 if pose0 is None else pose0)
+            self.acts.copy_(actions)
+            for s in range(self.A):
+                eng.tools_action(self.acts[s], self.vel[s * n], self.pose[s * n])
+        cur = self.ckpt[0]
+        for f in range(self.F):
+            if (f + 1) % self.k == 0:
+                nxt = self.ckpt[(f + 1) // self.k]
+            else:
+                nxt = self.seg[(f + 1) % 2]
+            eng.substep(cur, nxt, self.pose[f], self.pose[f + 1])
+            cur = nxt
+
+    def loss(self, targets: torch.Tensor, density_weight: float = 1.0, contact_weight: float = 0.0,
+             need_grad: bool = True) -> torch.Tensor:
+        """Density L1 (loss.py:172-175) per scene + optional soft contact (143-167)."""
+        eng = self.eng
+        final = self.final
+        eng.grid_mass(final, self.gm)
+        loss = eng.density_l1(self.gm, targets, density_weight, self.g_gm if need_grad else None)
+        g_final = self.g[0]
+        if need_grad:
+            g_final.zero_()
+            eng.grid_mass_bwd(final, self.g_gm, g_final)
+            self.g_pose.zero_()
+            self._loss_grad_ready = True
+        if contact_weight and eng.T:
+            md, sums = eng.soft_contact(final, self.pose[self.F])
+            movable = torch.tensor([float(t.action.dim > 0) for t in eng.tool_cfgs], dtype=torch.float64,
+                                   device=eng.device)
+            scene = torch.tensor(eng.tool_scene, device=eng.device)
+            loss = loss.index_add(0, scene, contact_weight * md * md * movable)
+            if need_grad:
+                g_md = (2 * contact_weight * md * movable).contiguous()
+                eng.soft_contact_bwd(final, self.pose[self.F], sums, g_md, g_final, self.g_pose[self.F])
+        return loss
+
+    def backward(self, g_final: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """Reverse sweep; returns d loss / d actions as [A, T, 8] (float64).
+
+        ``g_final`` defaults to the gradient left by ``loss`` (which also
+        seeds the pose gradients of the contact term); with an explicit
+        ``g_final`` and no preceding ``loss`` the pose gradients start at 0.
+        """
+        eng, n, k = self.eng, self.eng.n_sub, self.k
+        cur = self.g[0]
+        if g_final is not None:
+            cur.copy_(g_final)
+            if not getattr(self, "_loss_grad_ready", False):
+                self.g_pose.zero_()
+        elif not getattr(self, "_loss_grad_ready", False):
+            raise RuntimeError("Horizon.backward needs g_final or a preceding loss(need_grad=True)")
+        self._loss_grad_ready = False
+        nxt = self.g[1]
+        self.g_act.zero_()
+        for c in range(self.F // k - 1, -1, -1):
+            frames = [self.ckpt[c]]
+            for i in range(1, k):
+                dst = self.seg[i]
+                eng.substep(frames[-1], dst, self.pose[c * k + i - 1], self.pose[c * k + i])
+                frames.append(dst)
+            for i in range(k - 1, -1, -1):
+                f = c * k + i
+                eng.substep_bwd(frames[i], cur, nxt, self.pose[f], self.pose[f + 1], self.g_pose[f],
+                                self.g_pose[f + 1])
+                cur, nxt = nxt, cur
+        if eng.T:
+            for s in range(self.A - 1, -1, -1):
+                eng.tools_action_bwd(self.vel[s * n], self.pose[s * n], self.g_pose[s * n], self.g_act[s])
+        self.g_state0 = cur
+        return self.g_act

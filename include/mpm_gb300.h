@@ -1,0 +1,173 @@
+/*
+ * mpm_gb300.h -- C ABI of the GB300 (sm_103a) differentiable MLS-MPM substep.
+ *
+ * Drop-in boundary for the hot path of DiffSkill's plb/engine: the Taichi
+ * kernels of plb/engine/mpm_simulator.py (p2g, grid_op, g2p, compute_grid_m,
+ * their autodiff twins) and the tool kinematics of
+ * plb/engine/primitive/primive_base.py.  Host code (Python, ctypes) keeps the
+ * reference's API and owns all state buffers; this library receives raw
+ * device pointers and sizes, launches on the caller's CUDA stream, and never
+ * frees caller memory.  The only memory it owns is the per-handle grid
+ * scratch allocated by mpm_create and freed by mpm_destroy.
+ *
+ * Layouts (all device pointers, "real" = float or double per precision):
+ *   particle state of one frame: real[24][ld], component-major (SoA):
+ *       rows 0-2 x, 3-5 v, 6-14 C (row-major 3x3), 15-23 F (row-major 3x3);
+ *       particles of scene s occupy columns [scene_offsets[s], scene_offsets[s+1]).
+ *   grid (density, target): real[n_scenes][n_grid^3], node (i,j,k) at
+ *       (i*n + j)*n + k, the C order of the reference's 64^3 / 128^3 fields.
+ *   tool pose of one frame: double[n_tools][8] = pos[3], rot[4] (w,x,y,z), gap.
+ *   tool velocity of one substep: double[n_tools][8] = v[3], w[3], gap_vel, 0.
+ *   action of one step: double[n_tools][8] (first action_dim entries used).
+ *
+ * Every entry point returns 0 (MPM_OK) or an MPM_E_* code; mpm_last_error
+ * gives the message.  Kernels never trap: numerical faults and particles whose
+ * stencil leaves the grid set bits of a sticky device status word that
+ * mpm_status reads back.
+ */
+#ifndef MPM_GB300_H
+#define MPM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPM_ABI_VERSION 1
+
+/* return codes */
+#define MPM_OK 0
+#define MPM_E_INVALID 1   /* bad argument, size or pointer */
+#define MPM_E_CUDA 2      /* a CUDA runtime call failed */
+#define MPM_E_NOMEM 3     /* scratch allocation failed */
+
+/* precision modes (SIMULATOR.dtype of plb/config/default_config.py:15) */
+#define MPM_PREC_FP32 0       /* FP32 state/grid/SVD, FP64 reductions */
+#define MPM_PREC_FP32_SVD64 1 /* FP32 state/grid, FP64 SVD + return map + adjoint */
+#define MPM_PREC_FP64 2       /* all FP64: the plain reference method */
+
+/* tool types (plb/engine/primitive/primitives.py) */
+#define MPM_TOOL_SPHERE 0  /* Sphere   primitives.py:23-40 */
+#define MPM_TOOL_CAPSULE 1 /* Capsule  primitives.py:43-91 */
+#define MPM_TOOL_BOX 2     /* Box      primitives.py:359-425 */
+#define MPM_TOOL_KNIFE 3   /* Knife = Prism ∩ Box, primitives.py:700-815 */
+#define MPM_TOOL_GRIPPER 4 /* Gripper  primitives.py:428-573 */
+
+/* status bits (sticky; cleared by mpm_status with clear=1) */
+#define MPM_STATUS_OUT_OF_GRID 1u /* a particle stencil left the grid; it was skipped */
+#define MPM_STATUS_NONFINITE 2u   /* a NaN/Inf velocity or deformation was produced */
+
+/* Simulator constants: MPMSimulator.__init__ (mpm_simulator.py:8-67). */
+typedef struct MpmParams {
+  int32_t abi_version; /* MPM_ABI_VERSION */
+  int32_t precision;   /* MPM_PREC_* */
+  int32_t n_grid;      /* nodes per axis (64 or 128 in the workloads) */
+  int32_t n_scenes;    /* independent scenes batched in one launch */
+  int64_t n_particles; /* total over scenes */
+  int64_t ld;          /* leading dimension of state rows, >= n_particles */
+  double dx, inv_dx, dt, p_vol, p_mass;
+  double mu, lam, yield_stress; /* Lame parameters and von Mises yield */
+  double gravity[3];            /* multiplied by 30 in grid_op (mpm_simulator.py:235) */
+  double ground_friction;
+  double lower_bound;
+} MpmParams;
+
+/* One rigid tool: Primitive cfg (primive_base.py:313-329) + shape fields. */
+typedef struct MpmToolDesc {
+  int32_t type;       /* MPM_TOOL_* */
+  int32_t action_dim; /* cfg.action.dim */
+  int32_t scene;      /* owning scene; tools must be sorted by scene */
+  int32_t reserved;
+  double friction, softness;
+  double radius;        /* Sphere */
+  double cap_h, cap_r;  /* Capsule */
+  double size[3];       /* Box / Knife box / Gripper finger half extents */
+  double prism_h[2];    /* Knife prism h */
+  double prot[4];       /* Knife prism rotation */
+  double min_gap, max_gap;
+  double lower[3], upper[3];
+  double action_scale[7];
+} MpmToolDesc;
+
+typedef struct MpmHandle MpmHandle;
+
+const char* mpm_version(void);
+
+/* MPMSimulator.__init__ + initialize (mpm_simulator.py:8-97).
+ * scene_offsets: host int64[n_scenes+1], particle column ranges per scene.
+ * Allocates the grid scratch (4 grids of n_scenes*n_grid^3 nodes). */
+int mpm_create(const MpmParams* params, const int64_t* scene_offsets, MpmHandle** out);
+int mpm_destroy(MpmHandle* h);
+
+/* Primitives.__init__/initialize (primitives.py:820-897): tool table.
+ * tools: host array, sorted by scene; copied to the device. */
+int mpm_set_tools(MpmHandle* h, const MpmToolDesc* tools, int32_t n_tools);
+
+/* Primitive.set_action + set_velocity + forward_kinematics for the n_sub
+ * substeps of one action (primive_base.py:152-156, 246-274; Gripper
+ * primitives.py:457-469).  action: double[n_tools][8] (clipped by the caller);
+ * vel: double[n_sub][n_tools][8] written; pose: double[n_sub+1][n_tools][8]
+ * with frame 0 given, frames 1..n_sub written.  One launch. */
+int mpm_tools_action(MpmHandle* h, const double* action, double* vel, double* pose, int32_t n_sub,
+                     void* stream);
+/* Adjoint: set_velocity.grad + forward_kinematics.grad (function.py:180-182).
+ * g_pose: double[n_sub+1][n_tools][8] accumulated gradients of every frame on
+ * entry; on exit g_pose[0] also holds what reaches frame 0.  g_action:
+ * double[n_tools][8] accumulated. */
+int mpm_tools_action_bwd(MpmHandle* h, const double* vel, const double* pose, double* g_pose, double* g_action,
+                         int32_t n_sub, void* stream);
+
+/* One substep (MPMSimulator.substep, mpm_simulator.py:307-323, without the
+ * forward_kinematics that mpm_tools_action already ran): clear_grid,
+ * compute_F_tmp, svd, p2g, grid_op, g2p.  state_f -> state_f1 (distinct
+ * buffers).  pose_f, pose_f1: double[n_tools][8] of frames f and f+1. */
+int mpm_substep_fwd(MpmHandle* h, const void* state_f, void* state_f1, const double* pose_f, const double* pose_f1,
+                    void* stream);
+
+/* Adjoint of one substep (MPMSimulator.substep_grad, mpm_simulator.py:325-345:
+ * recompute grid, g2p.grad, grid_op.grad, p2g.grad, svd_grad,
+ * compute_F_tmp.grad).  g_state_f1 -> g_state_f (overwritten).
+ * g_pose_f, g_pose_f1: double[n_tools][8], accumulated. */
+int mpm_substep_bwd(MpmHandle* h, const void* state_f, const void* g_state_f1, void* g_state_f,
+                    const double* pose_f, const double* pose_f1, double* g_pose_f, double* g_pose_f1,
+                    void* stream);
+
+/* compute_grid_m_kernel on a cleared grid (mpm_simulator.py:456-471).
+ * grid_m: real[n_scenes][n_grid^3] written. */
+int mpm_grid_mass(MpmHandle* h, const void* state, void* grid_m, void* stream);
+/* compute_grid_m_kernel.grad (function.py:147-152): accumulates the x rows
+ * of g_state from g_grid_m (real[n_scenes][n_grid^3]). */
+int mpm_grid_mass_bwd(MpmHandle* h, const void* state, const void* g_grid_m, void* g_state, void* stream);
+
+/* compute_density_loss_kernel (loss.py:172-175) per scene, FP64 reduction:
+ * loss[s] = weight * sum_I |grid_m - target|  (double[n_scenes], overwritten);
+ * if g_grid_m is not NULL it receives weight * sgn(grid_m - target). */
+int mpm_density_l1(MpmHandle* h, const void* grid_m, const void* target, double weight, double* loss,
+                   void* g_grid_m, void* stream);
+
+/* Soft contact distance (loss.py:143-162) of every tool of every scene at one
+ * frame: min_dist[t] = sum_i d_i w_i / sum_i w_i, d_i = max(sdf_t(x_i), 0),
+ * w_i = 1/(1+1e4 d_i^2), over the particles of the tool's scene, in FP64.
+ * Tools with action_dim 0 are skipped (Loss keeps movable tools only,
+ * loss.py:21-25).  sums: double[n_tools][2] = (sum w, sum d w) written;
+ * min_dist: double[n_tools] written. */
+int mpm_soft_contact(MpmHandle* h, const void* state, const double* pose, double* sums, double* min_dist,
+                     void* stream);
+/* Adjoint given the forward sums and g_min_dist (double[n_tools]):
+ * accumulates the x rows of g_state and g_pose (double[n_tools][8]). */
+int mpm_soft_contact_bwd(MpmHandle* h, const void* state, const double* pose, const double* sums,
+                         const double* g_min_dist, void* g_state, double* g_pose, void* stream);
+
+/* Reads the sticky device status word (synchronises the stream). */
+int mpm_status(MpmHandle* h, uint32_t* status, int32_t clear, void* stream);
+/* Copies the last error message of this handle (or of mpm_create if h is NULL). */
+int mpm_last_error(MpmHandle* h, char* buf, size_t len);
+/* Number of kernel launches issued through this handle since creation. */
+int64_t mpm_launch_count(MpmHandle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPM_GB300_H */

@@ -1,0 +1,255 @@
+"""GPU (sm_103a) parity against the FP64 CPU oracle, through the C ABI.
+
+Tolerances (stated per test): the FP64 GPU path must match the oracle to
+near round-off (1e-9 relative per row group); FP32 paths are checked at the
+looser bounds that single precision allows (forward 1e-4 relative to the
+row-group magnitude, gradients 1e-3 / 5e-2 as stated below).
+"""
+import numpy as np
+import pytest
+import torch
+
+from _util import all_tools, group_errors, perturbed_state, rel_err, small_scene
+from diffskill_gb300.config import PrimitiveConfig
+from diffskill_gb300.engine import Horizon, MpmEngine
+from oracle.oracle import Oracle, init_state
+
+pytestmark = pytest.mark.gpu
+
+FWD_TOL = {"fp64": 1e-9, "fp32_svd64": 1e-4, "fp32": 1e-4}
+
+
+def to_soa(eng, aos):
+    st = eng.new_state()
+    st[:, :aos.shape[0]] = torch.as_tensor(aos.T, dtype=eng.dtype, device=eng.device)
+    return st
+
+
+def to_aos(eng, st, n=None):
+    n = eng.P if n is None else n
+    return st[:, :n].double().cpu().numpy().T.copy()
+
+
+def make_engine(sc, tools=None):
+    tools = sc.tools if tools is None else tools
+    return MpmEngine(sc.sim, [tools], [sc.n_particles])
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32_svd64", "fp32"])
+def test_substep_forward_matches_oracle(gpu_lib, prec):
+    tools = all_tools()
+    sc = small_scene(n=3000, tools=tools, precision=prec)
+    eng = make_engine(sc)
+    o = Oracle(sc.sim, tools)
+    st0 = perturbed_state(sc.x0, seed=3)
+    act = o.expand_action(sc.actions[0])
+    _, _, pseq = o.tools_action(o.pose0(), sc.actions[0])
+    ref = o.substep(pseq[0], pseq[1], st0)
+    pose = torch.as_tensor(pseq[:2], device=eng.device).contiguous()
+    s0, s1 = to_soa(eng, st0), eng.new_state()
+    eng.substep(s0, s1, pose[0], pose[1])
+    torch.cuda.synchronize()
+    assert eng.status() == 0
+    errs = group_errors(to_aos(eng, s1), ref)
+    assert max(errs.values()) < FWD_TOL[prec], errs
+    del act
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-8), ("fp32_svd64", 2e-3), ("fp32", 2e-3)])
+def test_substep_adjoint_matches_oracle(gpu_lib, prec, tol):
+    tools = all_tools()
+    sc = small_scene(n=3000, tools=tools, precision=prec)
+    eng = make_engine(sc)
+    o = Oracle(sc.sim, tools)
+    st0 = perturbed_state(sc.x0, seed=4)
+    _, _, pseq = o.tools_action(o.pose0(), sc.actions[0])
+    g1 = np.random.default_rng(5).normal(size=st0.shape)
+    gp_f, gp_f1 = np.zeros((o.T, 8)), np.zeros((o.T, 8))
+    ref = o.substep_bwd(pseq[0], pseq[1], st0, g1, gp_f, gp_f1)
+    pose = torch.as_tensor(pseq[:2], device=eng.device).contiguous()
+    gpose = torch.zeros((2, o.T, 8), dtype=torch.float64, device=eng.device)
+    s0, gg1, gg0 = to_soa(eng, st0), to_soa(eng, g1), eng.new_state()
+    eng.substep_bwd(s0, gg1, gg0, pose[0], pose[1], gpose[0], gpose[1])
+    torch.cuda.synchronize()
+    errs = group_errors(to_aos(eng, gg0), ref)
+    assert max(errs.values()) < tol, errs
+    gp = gpose.cpu().numpy()
+    assert rel_err(gp[0], gp_f) < tol * 10, (gp[0], gp_f)
+    assert rel_err(gp[1], gp_f1) < tol * 10, (gp[1], gp_f1)
+
+
+def test_tools_action_matches_oracle(gpu_lib):
+    tools = all_tools()
+    sc = small_scene(n=100, tools=tools, precision="fp64", substeps=20)
+    eng = make_engine(sc)
+    o = Oracle(sc.sim, tools)
+    acts, vel, pseq = o.tools_action(o.pose0(), sc.actions[0])
+    n = sc.sim.n_substeps
+    a = torch.zeros((o.T, 8), dtype=torch.float64, device=eng.device)
+    a[:, :7] = torch.as_tensor(acts, device=eng.device)
+    v = torch.zeros((n, o.T, 8), dtype=torch.float64, device=eng.device)
+    p = torch.zeros((n + 1, o.T, 8), dtype=torch.float64, device=eng.device)
+    p[0] = eng.pose0
+    eng.tools_action(a, v, p)
+    torch.cuda.synchronize()
+    assert rel_err(p.cpu().numpy(), pseq) < 1e-13
+    assert rel_err(v.cpu().numpy(), vel) < 1e-13
+    # adjoint
+    from oracle.oracle import lib, ptr
+    gps = np.random.default_rng(1).normal(size=pseq.shape)
+    g_ref, ga_ref = gps.copy(), np.zeros((o.T, 7))
+    lib().oracle_tools_action_bwd(o.tools, o.T, n, ptr(acts), ptr(vel), ptr(np.ascontiguousarray(pseq)), ptr(g_ref),
+                                  ptr(ga_ref))
+    g = torch.as_tensor(gps, device=eng.device).contiguous()
+    ga = torch.zeros((o.T, 8), dtype=torch.float64, device=eng.device)
+    eng.tools_action_bwd(v, p, g, ga)
+    torch.cuda.synchronize()
+    assert rel_err(g.cpu().numpy(), g_ref) < 1e-12
+    assert rel_err(ga.cpu().numpy()[:, :7], ga_ref) < 1e-12
+
+
+def _traj(eng, sc, k):
+    hz = Horizon(eng, sc.n_actions, ckpt_every=k)
+    st0 = eng.init_state([sc.x0])
+    acts = eng.expand_actions([sc.actions])
+    hz.forward(st0, acts)
+    tgt = eng.targets([sc.target])
+    loss = hz.loss(tgt, sc.density_weight, sc.contact_weight)
+    g = hz.backward()
+    torch.cuda.synchronize()
+    return float(loss.sum()), eng.collapse_action_grad(g)[0].cpu().numpy(), hz
+
+
+@pytest.mark.parametrize("prec,loss_tol,grad_tol", [("fp64", 1e-9, 1e-6), ("fp32_svd64", 1e-3, 5e-2),
+                                                    ("fp32", 1e-3, 5e-2)])
+def test_trajectory_loss_and_action_grad(gpu_lib, prec, loss_tol, grad_tol):
+    """Config-1 shape (capsule, density L1 to the +0.1-shifted dough), 2 actions x 50 substeps."""
+    sc = small_scene(n=4000, n_actions=2, substeps=50, precision=prec)
+    o = Oracle(sc.sim, sc.tools)
+    ref_loss, ref_grad = o.loss_and_grad(sc.x0, sc.actions, sc.target)
+    eng = make_engine(sc)
+    loss, grad, _ = _traj(eng, sc, k=10)
+    assert eng.status() == 0
+    assert abs(loss - ref_loss) / abs(ref_loss) < loss_tol, (loss, ref_loss)
+    assert rel_err(grad, ref_grad) < grad_tol, (grad, ref_grad)
+
+
+def test_checkpoint_recompute_equals_store_all(gpu_lib):
+    """Analogue of long_term_gradient.ipynb cell 4: checkpointed grad == full-tape grad."""
+    sc = small_scene(n=4000, n_actions=2, substeps=50, precision="fp64")
+    eng = make_engine(sc)
+    l1, g1, _ = _traj(eng, sc, k=1)
+    l2, g2, _ = _traj(eng, sc, k=10)
+    l3, g3, _ = _traj(eng, sc, k=50)
+    assert abs(l1 - l2) <= 1e-12 * abs(l1) and abs(l1 - l3) <= 1e-12 * abs(l1)
+    assert np.abs(g1 - g2).max() < 1e-4 and np.abs(g1 - g3).max() < 1e-4
+    assert rel_err(g2, g1) < 1e-9 and rel_err(g3, g1) < 1e-9
+
+
+def test_batched_scenes_equal_single_scenes(gpu_lib):
+    base = small_scene(n=1500, n_actions=1, substeps=20, precision="fp64")
+    scs = [small_scene(n=1000 + 500 * i, n_actions=1, substeps=20, precision="fp64", seed=2000 + i)
+           for i in range(3)]
+    tools = [[base.tools[0]], [all_tools()[2]], [all_tools()[0], all_tools()[4]]]
+    for sc, tl in zip(scs, tools):
+        sc.tools = tl
+        sc.actions = np.random.default_rng(len(tl)).uniform(-1, 1, size=(1, sum(t.action.dim for t in tl)))
+    eng = MpmEngine(base.sim, tools, [sc.n_particles for sc in scs])
+    hz = Horizon(eng, 1, ckpt_every=10)
+    hz.forward(eng.init_state([sc.x0 for sc in scs]), eng.expand_actions([sc.actions for sc in scs]))
+    loss = hz.loss(eng.targets([sc.target for sc in scs]))
+    g = eng.collapse_action_grad(hz.backward())
+    torch.cuda.synchronize()
+    for i, sc in enumerate(scs):
+        e1 = MpmEngine(sc.sim, [tools[i]], [sc.n_particles])
+        l1, g1, _ = _traj(e1, sc, k=10)
+        assert abs(float(loss[i]) - l1) <= 1e-12 * abs(l1)
+        assert rel_err(g[i].cpu().numpy(), g1) < 1e-9
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_grid_mass_and_density_l1(gpu_lib, prec):
+    sc = small_scene(n=5000, precision=prec)
+    eng = make_engine(sc)
+    o = Oracle(sc.sim, sc.tools)
+    st = perturbed_state(sc.x0, seed=9)
+    gm_ref = o.grid_mass(st)
+    s = to_soa(eng, st)
+    gm = eng.grid_mass(s)
+    tgt = eng.targets([sc.target])
+    g_gm = torch.empty_like(gm)
+    loss = eng.density_l1(gm, tgt, 1.0, g_gm)
+    torch.cuda.synchronize()
+    tol = 1e-12 if prec == "fp64" else 1e-5
+    assert rel_err(gm.cpu().numpy()[0], gm_ref) < tol
+    assert abs(gm.double().sum().item() - sc.n_particles * sc.sim.p_mass) < 1e-6 * sc.n_particles * sc.sim.p_mass
+    ref_loss = float(np.abs(gm_ref - sc.target).sum())
+    assert abs(float(loss[0]) - ref_loss) < (1e-10 if prec == "fp64" else 1e-4) * ref_loss
+    g_ref = np.zeros_like(st)
+    o.grid_mass_bwd(st, np.sign(gm_ref - sc.target), g_ref)
+    gs = eng.new_state()
+    eng.grid_mass_bwd(s, g_gm, gs)
+    torch.cuda.synchronize()
+    got = to_aos(eng, gs)[:, 0:3]
+    if prec == "fp64":
+        assert rel_err(got, g_ref[:, 0:3]) < 1e-9
+    else:  # sign flips where |m - target| ~ FP32 rounding change a few nodes
+        assert np.mean(np.abs(got - g_ref[:, 0:3]) < 1e-3 * np.abs(g_ref[:, 0:3]).max()) > 0.99
+
+
+def test_soft_contact_matches_oracle(gpu_lib):
+    tools = all_tools()
+    sc = small_scene(n=3000, tools=tools, precision="fp64")
+    eng = make_engine(sc)
+    o = Oracle(sc.sim, tools)
+    st = perturbed_state(sc.x0, seed=2)
+    pose = o.pose0()
+    s = to_soa(eng, st)
+    pz = torch.as_tensor(pose, device=eng.device).contiguous()
+    md, sums = eng.soft_contact(s, pz)
+    g_md = torch.arange(1, o.T + 1, dtype=torch.float64, device=eng.device)
+    gs = eng.new_state()
+    gp = torch.zeros((o.T, 8), dtype=torch.float64, device=eng.device)
+    eng.soft_contact_bwd(s, pz, sums, g_md, gs, gp)
+    torch.cuda.synchronize()
+    g_ref, gp_ref = np.zeros_like(st), np.zeros((o.T, 8))
+    for t in range(o.T):
+        ref = o.soft_contact(t, pose[t], st)
+        assert abs(float(md[t]) - ref) < 1e-10 * max(abs(ref), 1e-12)
+        gpt = np.zeros(8)
+        o.soft_contact(t, pose[t], st, float(t + 1), g_ref, gpt)
+        gp_ref[t] = gpt
+    assert rel_err(to_aos(eng, gs)[:, 0:3], g_ref[:, 0:3]) < 1e-9
+    assert rel_err(gp.cpu().numpy(), gp_ref) < 1e-9
+
+
+def test_out_of_grid_particle_sets_status_and_is_skipped(gpu_lib):
+    """A particle outside [0, 1-3dx] is bounds-checked on the device: its
+    scatter is skipped, the sticky status bit is set, nothing faults."""
+    sc = small_scene(n=500, precision="fp32")
+    eng = make_engine(sc)
+    x = sc.x0.copy()
+    x[7] = [1.5, 0.5, 0.5]
+    s0 = eng.init_state([x])
+    s1 = eng.new_state()
+    pose = eng.pose0.unsqueeze(0).repeat(2, 1, 1).contiguous()
+    eng.substep(s0, s1, pose[0], pose[1])
+    st = eng.status(clear=True)
+    assert st & 1
+    assert eng.status(clear=True) == 0
+    got = s1[:3, 7].cpu().numpy()
+    assert np.allclose(got, [1.5, 0.5, 0.5])
+
+
+def test_invalid_arguments_raise(gpu_lib):
+    from diffskill_gb300 import _lib
+    sc = small_scene(n=100, precision="fp32")
+    eng = make_engine(sc)
+    s0 = eng.new_state()
+    with pytest.raises(_lib.MpmError, match="must differ"):
+        eng.substep(s0, s0, eng.pose0, eng.pose0)
+    bad = PrimitiveConfig(shape="Box")
+    bad_sim = sc.sim
+    bad_sim.n_grid = 60
+    with pytest.raises(_lib.MpmError, match="multiple of 8"):
+        MpmEngine(bad_sim, [[bad]], [10])

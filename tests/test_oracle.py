@@ -1,0 +1,288 @@
+"""CPU tests of the FP64 oracle: golden vectors from the reference, SVD,
+SDF/normal property, and the hand adjoint against central differences."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from _util import all_tools, perturbed_state, small_scene
+from diffskill_gb300 import scenes
+from oracle import oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "density_assets.json")
+
+
+@pytest.fixture(scope="module")
+def golden():
+    with open(GOLDEN) as fh:
+        return json.load(fh)
+
+
+# --------------------------------------------------------------------------
+# golden vectors: the reference's density assets (plb/envs/assets/*.npy)
+# --------------------------------------------------------------------------
+def test_assets_pin_particle_mass(golden):
+    """Every asset holds 10000 particles of p_mass=(dx/2)^2 (mpm_simulator.py:28-29)."""
+    sim = scenes.config1().sim
+    assert sim.p_mass == (0.5 / 64) ** 2
+    for name, g in golden["grids"].items():
+        assert g["n_grid"] == 64
+        assert abs(g["total_mass"] - 10000 * sim.p_mass) < 1e-12, name
+
+
+def test_oracle_grid_mass_reproduces_move3d_asset(golden):
+    """Oracle compute_grid_m of a seeded sphere sample, placed like the
+    Move3D-v1 target, matches the asset's mass, support and moments."""
+    g = golden["grids"]["Move3D-v1.npy"]
+    r = golden["move3d_v1_sphere_radius"]
+    sc = scenes.config1(n_particles=10)
+    rng = np.random.default_rng(77)
+    x = scenes.sample_sphere(rng, 10000, (0, 0, 0), r)
+    x = x - x.mean(0) + np.array(g["centroid"])  # same centroid as the asset
+    o = O.Oracle(sc.sim, [])
+    gm = o.grid_mass(O.init_state(x)).reshape(64, 64, 64)
+    dx = 1 / 64
+    idx = np.indices(gm.shape).reshape(3, -1).T * dx
+    m = gm.reshape(-1)
+    tot = m.sum()
+    assert abs(tot - g["total_mass"]) < 1e-12
+    cen = (m[:, None] * idx).sum(0) / tot
+    assert np.abs(cen - x.mean(0)).max() < 1e-12  # linear reproduction of the B-spline
+    var = (m[:, None] * (idx - cen) ** 2).sum(0) / tot
+    assert np.abs(var - x.var(0) - dx * dx / 4).max() < 1e-12  # B-spline variance dx^2/4
+    # against the asset: same support box (+-1 node) and moments within sampling noise
+    nz = np.argwhere(gm > 0)
+    assert np.abs(nz.min(0) - np.array(g["support_min"])).max() <= 1
+    assert np.abs(nz.max(0) - np.array(g["support_max"])).max() <= 1
+    assert abs(var.mean() - np.mean(g["var"])) < 0.03 * np.mean(g["var"])
+    assert abs(gm.max() - g["max"]) < 0.15 * g["max"]
+
+
+# --------------------------------------------------------------------------
+# SVD (ti.svd convention, mpm_simulator.py:127-129) and backward_svd (137-156)
+# --------------------------------------------------------------------------
+def _svd(A):
+    U, s, V = np.zeros(9), np.zeros(3), np.zeros(9)
+    O.lib().oracle_svd(O.ptr(np.ascontiguousarray(A.reshape(9))), O.ptr(U), O.ptr(s), O.ptr(V))
+    return U.reshape(3, 3), s, V.reshape(3, 3)
+
+
+@pytest.mark.parametrize("kind", ["random", "near_rotation", "reflection", "degenerate", "identity"])
+def test_svd_convention(kind):
+    rng = np.random.default_rng(0)
+    for _ in range(50):
+        if kind == "random":
+            A = rng.normal(size=(3, 3))
+        elif kind == "near_rotation":
+            q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+            A = q * np.sign(np.linalg.det(q)) + 1e-3 * rng.normal(size=(3, 3))
+        elif kind == "reflection":
+            A = np.diag([1.0, 1.0, -1.0]) @ rng.normal(size=(3, 3))
+            if np.linalg.det(A) > 0:
+                A[2] *= -1
+        elif kind == "degenerate":
+            q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+            A = q @ np.diag([1.0, 1.0, 0.5]) @ q.T
+        else:
+            A = np.eye(3)
+        U, s, V = _svd(A)
+        assert np.allclose(U @ np.diag(s) @ V.T, A, atol=1e-12)
+        assert np.allclose(U.T @ U, np.eye(3), atol=1e-12) and np.allclose(V.T @ V, np.eye(3), atol=1e-12)
+        assert abs(np.linalg.det(U) - 1) < 1e-12 and abs(np.linalg.det(V) - 1) < 1e-12
+        assert s[0] >= s[1] - 1e-14 and s[1] >= abs(s[2]) - 1e-14
+        assert np.sign(s[2]) == np.sign(np.linalg.det(A)) or abs(s[2]) < 1e-12
+
+
+def test_svd_backward_matches_finite_differences():
+    """With well separated singular values the clamped formula is the exact VJP."""
+    rng = np.random.default_rng(1)
+    for _ in range(20):
+        q1, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        q2, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        A = q1 @ np.diag([1.6, 1.1, 0.7]) @ q2.T
+        gU, gs, gV = rng.normal(size=9), rng.normal(size=3), rng.normal(size=9)
+        U, s, V = _svd(A)
+        gA = np.zeros(9)
+        O.lib().oracle_svd_bwd(O.ptr(U.reshape(9).copy()), O.ptr(s), O.ptr(V.reshape(9).copy()), O.ptr(gU),
+                               O.ptr(gs), O.ptr(gV), O.ptr(gA))
+
+        def f(M):
+            u, ss, v = _svd(M)
+            return gU @ u.reshape(9) + gs @ ss + gV @ v.reshape(9)
+
+        fd = np.zeros(9)
+        for i in range(9):
+            e = np.zeros(9)
+            e[i] = 1e-6
+            fd[i] = (f(A + e.reshape(3, 3)) - f(A - e.reshape(3, 3))) / 2e-6
+        assert np.abs(fd - gA).max() < 1e-6 * max(1, np.abs(gA).max())
+
+
+def test_svd_backward_clamp_at_identity():
+    """F = I: s_j^2 - s_i^2 = 0 is clamped to +1e-6 (mpm_simulator.py:184-192), and the
+    rotation terms cancel exactly for a gradient that only flows through R = U V^T."""
+    U, s, V = _svd(np.eye(3))
+    gR = np.random.default_rng(2).normal(size=(3, 3))
+    gU, gV = gR @ V, gR.T @ U
+    gA = np.zeros(9)
+    O.lib().oracle_svd_bwd(O.ptr(U.reshape(9).copy()), O.ptr(s), O.ptr(V.reshape(9).copy()),
+                           O.ptr(gU.reshape(9).copy()), O.ptr(np.zeros(3)), O.ptr(gV.reshape(9).copy()), O.ptr(gA))
+    assert np.abs(gA).max() < 1e-9
+
+
+# --------------------------------------------------------------------------
+# SDF / normal property (plb/engine/primitive/test_primitives.py:34-67)
+# --------------------------------------------------------------------------
+@pytest.mark.parametrize("ti", range(5))
+def test_tool_normal_matches_sdf_gradient(ti):
+    tool = all_tools()[ti]
+    ts = O.tool_struct(tool, 666.0)
+    pose = np.array(tool.init_state, dtype=np.float64)
+    # Primitive.normal rotates by the stored quaternion without normalising it
+    # (primive_base.py:85); the property holds exactly for unit quaternions.
+    pose[3:7] /= np.linalg.norm(pose[3:7])
+    rng = np.random.default_rng(ti)
+    pts = pose[:3] + rng.normal(size=(400, 3)) * 0.06
+    sdf, nrm = np.zeros(400), np.zeros((400, 3))
+    O.lib().oracle_tool_sdf(ctypes_ref(ts), O.ptr(pose), 400, O.ptr(pts), O.ptr(sdf), O.ptr(nrm))
+    fd = np.zeros((400, 3))
+    for k in range(3):
+        e = np.zeros(3)
+        e[k] = 1e-7
+        sp, sm = np.zeros(400), np.zeros(400)
+        O.lib().oracle_tool_sdf(ctypes_ref(ts), O.ptr(pose), 400, O.ptr(pts + e), O.ptr(sp), None)
+        O.lib().oracle_tool_sdf(ctypes_ref(ts), O.ptr(pose), 400, O.ptr(pts - e), O.ptr(sm), None)
+        fd[:, k] = (sp - sm) / 2e-7
+    fdn = fd / np.linalg.norm(fd, axis=1, keepdims=True)
+    err = np.linalg.norm(fdn - nrm, axis=1)
+    if tool.shape in ("Sphere", "Capsule"):
+        assert np.median(err) < 1e-5 and np.mean(err < 1e-5) > 0.95
+    else:  # FD normal with d=1e-4: agrees away from edges and corners
+        assert np.mean(err < 1e-3) > 0.8
+
+
+def ctypes_ref(s):
+    import ctypes
+    return ctypes.byref(s)
+
+
+# --------------------------------------------------------------------------
+# the hand adjoint against FP64 central differences
+# --------------------------------------------------------------------------
+def _fd_best(f, x0, i, eps_list=(1e-3, 1e-4, 1e-5, 1e-6)):
+    vals = []
+    for eps in eps_list:
+        xp, xm = x0.copy(), x0.copy()
+        xp.flat[i] += eps
+        xm.flat[i] -= eps
+        vals.append((f(xp) - f(xm)) / (2 * eps))
+    return vals
+
+
+@pytest.mark.parametrize("ti", range(5))
+def test_substep_adjoint_matches_finite_differences(ti):
+    tools = [all_tools()[ti]]
+    sc = small_scene(n=250, substeps=3, tools=tools, precision="fp64")
+    sc.sim.yield_stress = 5.0  # exercise the plastic branch
+    o = O.Oracle(sc.sim, tools)
+    st0 = perturbed_state(sc.x0, seed=ti)
+    rng = np.random.default_rng(100 + ti)
+    W = rng.normal(size=st0.shape)
+    a = sc.actions[0]
+    K = sc.sim.n_substeps
+
+    def run(st, act, frames=None):
+        _, _, pseq = o.tools_action(o.pose0(), act)
+        s = st
+        for j in range(K):
+            if frames is not None:
+                frames.append(s)
+            s = o.substep(pseq[j], pseq[j + 1], s)
+        return float((W * s).sum()), pseq
+
+    frames = []
+    _, pseq = run(st0, a, frames)
+    g = W.copy()
+    gp = np.zeros((K + 1, o.T, 8))
+    for f in range(K - 1, -1, -1):
+        g = o.substep_bwd(pseq[f], pseq[f + 1], frames[f], g, gp[f], gp[f + 1])
+    idx = [int(i) for i in rng.integers(0, st0.size, size=12)]
+    for i in idx:
+        fds = _fd_best(lambda s: run(s, a)[0], st0, i)
+        best = min(abs(v - g.flat[i]) / max(abs(v), 1e-8) for v in fds)
+        assert best < 1e-5, (i, g.flat[i], fds)
+
+
+def test_tools_action_adjoint_matches_finite_differences():
+    tools = all_tools()
+    sc = small_scene(n=10, substeps=7, tools=tools, precision="fp64")
+    o = O.Oracle(sc.sim, tools)
+    a = sc.actions[0]
+    rng = np.random.default_rng(3)
+    W = rng.normal(size=(sc.sim.n_substeps + 1, o.T, 8))
+
+    def f(act):
+        return float((W * o.tools_action(o.pose0(), act)[2]).sum())
+
+    acts, vel, pseq = o.tools_action(o.pose0(), a)
+    gp = W.copy()
+    ga = np.zeros((o.T, 7))
+    O.lib().oracle_tools_action_bwd(o.tools, o.T, sc.sim.n_substeps, O.ptr(acts), O.ptr(vel),
+                                    O.ptr(np.ascontiguousarray(pseq)), O.ptr(gp), O.ptr(ga))
+    flat = np.concatenate([ga[i, :o.dims[i + 1] - o.dims[i]] for i in range(o.T)])
+    for k in range(len(a)):
+        fds = _fd_best(f, a, k, (1e-5, 1e-6))
+        best = min(abs(v - flat[k]) / max(abs(v), 1e-8) for v in fds)
+        assert best < 1e-6, (k, flat[k], fds)
+
+
+def test_trajectory_action_gradient_matches_finite_differences():
+    sc = small_scene(n=300, n_actions=2, substeps=5, precision="fp64")
+    sc.tools[0].action.scale = (0.05, 0.05, 0.05)
+    o = O.Oracle(sc.sim, sc.tools)
+    loss, grad = o.loss_and_grad(sc.x0, sc.actions, sc.target)
+    W = sc.actions.copy()
+    for i in range(W.size):
+        fds = _fd_best(lambda A: o.loss(o.rollout(sc.x0, A, keep_frames=False)["final"], sc.target), W, i,
+                       (1e-6, 1e-7))
+        best = min(abs(v - grad.flat[i]) / max(abs(v), 1e-6) for v in fds)
+        assert best < 1e-4, (i, grad.flat[i], fds)
+
+
+def test_grid_mass_conserves_particle_mass():
+    sc = small_scene(n=3000, precision="fp64")
+    o = O.Oracle(sc.sim, sc.tools)
+    gm = o.grid_mass(perturbed_state(sc.x0))
+    assert abs(gm.sum() - 3000 * sc.sim.p_mass) < 1e-14
+
+
+def test_oracle_is_deterministic_across_thread_counts():
+    sc = small_scene(n=2000, precision="fp64", tools=all_tools())
+    o = O.Oracle(sc.sim, sc.tools)
+    st0 = perturbed_state(sc.x0, seed=1)
+    _, _, pseq = o.tools_action(o.pose0(), sc.actions[0])
+    n0 = O.num_threads()
+    try:
+        O.set_num_threads(1)
+        a = o.substep(pseq[0], pseq[1], st0)
+        ga = o.substep_bwd(pseq[0], pseq[1], st0, st0, np.zeros((o.T, 8)), np.zeros((o.T, 8)))
+        O.set_num_threads(4)
+        b = o.substep(pseq[0], pseq[1], st0)
+        gb = o.substep_bwd(pseq[0], pseq[1], st0, st0, np.zeros((o.T, 8)), np.zeros((o.T, 8)))
+    finally:
+        O.set_num_threads(n0)
+    assert np.array_equal(a, b) and np.array_equal(ga, gb)
+
+
+def test_baseline_config1_time_step_diverges():
+    """The benchmark definition's dt=5e-4 exceeds the CFL limit dx/c ~ 2.1e-4
+    (c = sqrt((lam+2mu)/rho) ~ 74.5): the FP64 oracle produces NaN; the
+    reference's own dt=1e-4 (mpm_simulator.py:27) stays finite."""
+    sc = scenes.config1(n_actions=4, n_particles=2000, dt=5e-4, substeps=50)
+    o = O.Oracle(sc.sim, sc.tools)
+    fin = o.rollout(sc.x0, sc.actions, keep_frames=False)["final"]
+    assert not np.isfinite(fin[:, 3:]).all()
+    sc = scenes.config1(n_actions=4, n_particles=2000, dt=1e-4, substeps=50)
+    fin = O.Oracle(sc.sim, sc.tools).rollout(sc.x0, sc.actions, keep_frames=False)["final"]
+    assert np.isfinite(fin).all()
