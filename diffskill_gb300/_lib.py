@@ -58,10 +58,18 @@ SIGNATURES = {
     "mpm_density_l1": (_i32, [_c_p, _c_p, _c_p, _f64, _c_p, _c_p, _c_p]),
     "mpm_soft_contact": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_soft_contact_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
+    "mpm_tool_distance_cols": (_i32, [_c_p]),
+    "mpm_tool_distance": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p]),
+    "mpm_tool_distance_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_status": (_i32, [_c_p, ctypes.POINTER(ctypes.c_uint32), _i32, _c_p]),
     "mpm_last_error": (_i32, [_c_p, ctypes.c_char_p, ctypes.c_size_t]),
     "mpm_launch_count": (_i64, [_c_p]),
+    "mpm_profile_enable": (_i32, [_c_p, _i32]),
+    "mpm_profile_read": (_i32, [_c_p, ctypes.POINTER(_f64), ctypes.POINTER(_i64)]),
 }
+
+# kernel kinds of mpm_profile_read (MPM_K_* in the header)
+KERNEL_KINDS = ["p2g", "p2g_recompute", "grid_op", "g2p", "g2p_adj", "grid_op_adj", "p2g_adj", "clear", "other"]
 
 _lib: Optional[ctypes.CDLL] = None
 

@@ -21,27 +21,18 @@ cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* g1, T*
   Node<T>* g_gout = (Node<T>*)L.grid_d;
   const unsigned pb = blocks_for(c.n_particles, 128);
   // recompute the grid of this substep (substep_grad, mpm_simulator.py:327-333)
-  cudaError_t e = cudaMemsetAsync(gin, 0, nodes * sizeof(Node<T>), L.stream);
-  if (e != cudaSuccess) return e;
-  if (c.n_particles > 0) {
-    k_p2g<T, S><<<pb, 128, 0, L.stream>>>(c, st0, (T*)nullptr, L.pscene, gin);
-    ++*L.launches;
-  }
-  k_grid_op<T><<<(unsigned)(nodes / 128), 128, 0, L.stream>>>(c, gin, gout, L.tools, L.tool_off, pose_f, pose_f1);
-  ++*L.launches;
-  e = cudaMemsetAsync(g_gout, 0, nodes * sizeof(Node<T>), L.stream);
-  if (e != cudaSuccess) return e;
-  if (c.n_particles > 0) {
-    k_g2p_adj<T><<<pb, 128, 0, L.stream>>>(c, st0, g1, g0, L.pscene, gout, g_gout);
-    ++*L.launches;
-  }
-  k_grid_op_adj<T><<<(unsigned)(nodes / 128), 128, 0, L.stream>>>(c, gin, g_gout, g_gin, L.tools, L.tool_off, pose_f,
-                                                                  pose_f1, g_pose_f, g_pose_f1);
-  ++*L.launches;
-  if (c.n_particles > 0) {
-    k_p2g_adj<T, S><<<pb, 128, 0, L.stream>>>(c, st0, g1, g0, L.pscene, g_gin);
-    ++*L.launches;
-  }
+  MPM_MEMSET(L, gin, nodes * sizeof(Node<T>));
+  if (c.n_particles > 0)
+    MPM_LAUNCH(L, MPM_K_P2G_RECOMP, (k_p2g<T, S>), pb, 128, c, st0, (T*)nullptr, L.pscene, gin);
+  MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, (unsigned)(nodes / 128), 128, c, gin, gout, L.tools, L.tool_off,
+             pose_f, pose_f1);
+  MPM_MEMSET(L, g_gout, nodes * sizeof(Node<T>));
+  if (c.n_particles > 0)
+    MPM_LAUNCH(L, MPM_K_G2P_ADJ, k_g2p_adj<T>, pb, 128, c, st0, g1, g0, L.pscene, gout, g_gout);
+  MPM_LAUNCH(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, (unsigned)(nodes / 128), 128, c, gin, g_gout, g_gin, L.tools,
+             L.tool_off, pose_f, pose_f1, g_pose_f, g_pose_f1);
+  if (c.n_particles > 0)
+    MPM_LAUNCH(L, MPM_K_P2G_ADJ, (k_p2g_adj<T, S>), pb, 128, c, st0, g1, g0, L.pscene, g_gin);
   return cudaGetLastError();
 }
 
@@ -91,13 +82,79 @@ cudaError_t launch_soft_contact_bwd(const LaunchCtx& L, int n_tools, const T* st
                                     const double* sums, const double* g_min, T* gst, double* g_pose) {
   (void)n_tools;
   Consts<T> c = make_consts<T>(L);
-  if (c.n_particles > 0) {
-    k_contact_adj<T><<<blocks_for(c.n_particles, 128), 128, 0, L.stream>>>(c, st, L.pscene, L.tools, L.tool_off,
-                                                                             pose, sums, g_min, gst, g_pose);
-    ++*L.launches;
-  }
+  if (c.n_particles > 0)
+    MPM_LAUNCH(L, MPM_K_OTHER, k_contact_adj<T>, blocks_for(c.n_particles, 128), 128, c, st, L.pscene, L.tools,
+               L.tool_off, pose, sums, g_min, gst, g_pose);
   return cudaGetLastError();
 }
+
+// tool distance adjoint (compute_min_dist.grad, function.py:154-159)
+template <typename T>
+__global__ void __launch_bounds__(128) k_tool_distance_adj(Consts<T> c, const T* __restrict__ st,
+                                                           const int* __restrict__ pscene,
+                                                           const MpmToolDesc* __restrict__ tools,
+                                                           const int* __restrict__ tool_off,
+                                                           const int* __restrict__ col_off,
+                                                           const double* __restrict__ pose,
+                                                           const T* __restrict__ g_out, T* __restrict__ gst,
+                                                           double* __restrict__ g_pose) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= c.n_particles) return;
+  int sc = pscene[p];
+  T x[3];
+  load_row(st, c.ld, p, 0, 3, x);
+  T gx[3] = {T(0), T(0), T(0)};
+  for (int t = tool_off[sc]; t < tool_off[sc + 1]; ++t) {
+    Tool<T> tl;
+    Pose<T> P;
+    to_tool(tools[t], tl);
+    to_pose(pose + 8 * t, P);
+    const int col = col_off[t];
+    PoseGrad<T> gP;
+    gP.zero();
+    bool any = false;
+    if (tl.type == TOOL_GRIPPER) {
+#pragma unroll
+      for (int side = 0; side < 2; ++side) {
+        T g = g_out[(int64_t)(col + side) * c.ld + p];
+        if (g == T(0)) continue;
+        any = true;
+        T flag = side == 0 ? T(-1) : T(1);
+        T fp[3], gf[3] = {T(0), T(0), T(0)};
+        finger_pos(P, flag, fp);
+        shape_sdf_vjp(tl, fp, P.rot, x, g, gx, gf, gP.rot);
+        finger_pos_vjp(P, flag, gf, gP);
+      }
+    } else {
+      T g = g_out[(int64_t)col * c.ld + p];
+      if (g != T(0)) {
+        any = true;
+        tool_sdf_vjp(tl, P, x, g, gx, gP);
+      }
+    }
+    if (any) {
+      for (int k = 0; k < 3; ++k) atomicAdd(g_pose + 8 * t + k, double(gP.pos[k]));
+      for (int k = 0; k < 4; ++k) atomicAdd(g_pose + 8 * t + 3 + k, double(gP.rot[k]));
+      atomicAdd(g_pose + 8 * t + 7, double(gP.gap));
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) gst[(int64_t)d * c.ld + p] += gx[d];
+}
+
+template <typename T>
+cudaError_t launch_tool_distance_bwd(const LaunchCtx& L, const int* col_off, const T* st, const double* pose,
+                                     const T* g_out, T* gst, double* g_pose) {
+  Consts<T> c = make_consts<T>(L);
+  if (c.n_particles > 0)
+    MPM_LAUNCH(L, MPM_K_OTHER, k_tool_distance_adj<T>, blocks_for(c.n_particles, 128), 128, c, st, L.pscene,
+               L.tools, L.tool_off, col_off, pose, g_out, gst, g_pose);
+  return cudaGetLastError();
+}
+template cudaError_t launch_tool_distance_bwd<float>(const LaunchCtx&, const int*, const float*, const double*,
+                                                     const float*, float*, double*);
+template cudaError_t launch_tool_distance_bwd<double>(const LaunchCtx&, const int*, const double*, const double*,
+                                                      const double*, double*, double*);
 
 #define MPM_INST_BWD(T, S)                                                                                  \
   template cudaError_t launch_substep_bwd<T, S>(const LaunchCtx&, const T*, const T*, T*, const double*, \

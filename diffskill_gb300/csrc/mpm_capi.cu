@@ -19,6 +19,8 @@ struct MpmHandle {
   std::vector<int64_t> offsets;
   int* d_pscene = nullptr;
   int* d_tool_off = nullptr;
+  int* d_col_off = nullptr;  // first tool-distance column of each tool
+  int n_cols = 0;
   MpmToolDesc* d_tools = nullptr;
   int n_tools = 0;
   std::vector<MpmToolDesc> h_tools;
@@ -26,7 +28,27 @@ struct MpmHandle {
   void* grid[4] = {nullptr, nullptr, nullptr, nullptr};
   std::string err;
   int64_t launches = 0;
+  mpm::Profiler prof;
+  std::vector<cudaEvent_t> events;  // event pool of the profiler
+  std::vector<mpm::Profiler::Rec> recs;
 };
+
+namespace mpm {
+int prof_begin(Profiler* P, cudaStream_t s) {
+  if (!P || !P->on) return -1;
+  if (P->pool_n + 2 > P->pool_cap) return -1;  // pool exhausted: drop this sample
+  cudaEvent_t a = P->pool[P->pool_n];
+  if (cudaEventRecord(a, s) != cudaSuccess) return -1;
+  return P->pool_n;
+}
+void prof_end(Profiler* P, int slot, int kind, cudaStream_t s) {
+  if (slot < 0 || !P || P->n >= P->cap) return;
+  cudaEvent_t b = P->pool[slot + 1];
+  if (cudaEventRecord(b, s) != cudaSuccess) return;
+  P->recs[P->n++] = Profiler::Rec{kind, P->pool[slot], b};
+  P->pool_n = slot + 2;
+}
+}  // namespace mpm
 
 namespace {
 
@@ -61,6 +83,7 @@ mpm::LaunchCtx ctx(MpmHandle* h, void* stream) {
   L.grid_d = h->grid[3];
   L.stream = (cudaStream_t)stream;
   L.launches = &h->launches;
+  L.prof = &h->prof;
   return L;
 }
 int check_device(MpmHandle* h) {
@@ -240,9 +263,11 @@ int mpm_destroy(MpmHandle* h) {
   if (!h) return MPM_OK;
   cudaFree(h->d_pscene);
   cudaFree(h->d_tool_off);
+  cudaFree(h->d_col_off);
   cudaFree(h->d_tools);
   cudaFree(h->d_status);
   for (int i = 0; i < 4; ++i) cudaFree(h->grid[i]);
+  for (cudaEvent_t e : h->events) cudaEventDestroy(e);
   delete h;
   return MPM_OK;
 }
@@ -270,14 +295,26 @@ int mpm_set_tools(MpmHandle* h, const MpmToolDesc* tools, int32_t n_tools) {
                                         " tools in scene " + std::to_string(s));
     toff[s + 1] += toff[s];
   }
+  std::vector<int> coff(std::max(n_tools, 1), 0);
+  int ncols = 0;
+  for (int i = 0; i < n_tools; ++i) {
+    coff[i] = ncols;
+    ncols += tools[i].type == MPM_TOOL_GRIPPER ? 2 : 1;
+  }
   cudaError_t e = cudaSuccess;
   if (n_tools > h->n_tools) {
     cudaFree(h->d_tools);
+    cudaFree(h->d_col_off);
     h->d_tools = nullptr;
+    h->d_col_off = nullptr;
     e = cudaMalloc(&h->d_tools, n_tools * sizeof(MpmToolDesc));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_col_off, n_tools * sizeof(int));
     if (e != cudaSuccess) return cuda_fail(h, e, "mpm_set_tools: cudaMalloc");
   }
   if (n_tools > 0) e = cudaMemcpy(h->d_tools, tools, n_tools * sizeof(MpmToolDesc), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && n_tools > 0)
+    e = cudaMemcpy(h->d_col_off, coff.data(), n_tools * sizeof(int), cudaMemcpyHostToDevice);
+  h->n_cols = ncols;
   if (e == cudaSuccess) e = cudaMemcpy(h->d_tool_off, toff.data(), toff.size() * sizeof(int), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(h, e, "mpm_set_tools: upload");
   h->n_tools = n_tools;
@@ -453,6 +490,43 @@ int mpm_soft_contact_bwd(MpmHandle* h, const void* state, const double* pose, co
   return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_soft_contact_bwd");
 }
 
+int mpm_tool_distance_cols(MpmHandle* h) { return h ? h->n_cols : 0; }
+
+int mpm_tool_distance(MpmHandle* h, const void* state, const double* pose, void* out, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_tool_distance: NULL handle");
+  if (h->n_tools == 0) return MPM_OK;
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, state, "state"));
+  MPM_TRY(check_aligned(h, pose, "pose"));
+  MPM_TRY(check_aligned(h, out, "out"));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e = h->p.precision == MPM_PREC_FP64
+                      ? mpm::launch_tool_distance<double>(L, h->d_col_off, h->n_cols, (const double*)state, pose,
+                                                          (double*)out)
+                      : mpm::launch_tool_distance<float>(L, h->d_col_off, h->n_cols, (const float*)state, pose,
+                                                         (float*)out);
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_tool_distance");
+}
+
+int mpm_tool_distance_bwd(MpmHandle* h, const void* state, const double* pose, const void* g_out, void* g_state,
+                          double* g_pose, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_tool_distance_bwd: NULL handle");
+  if (h->n_tools == 0) return MPM_OK;
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, state, "state"));
+  MPM_TRY(check_aligned(h, pose, "pose"));
+  MPM_TRY(check_aligned(h, g_out, "g_out"));
+  MPM_TRY(check_aligned(h, g_state, "g_state"));
+  MPM_TRY(check_aligned(h, g_pose, "g_pose"));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e = h->p.precision == MPM_PREC_FP64
+                      ? mpm::launch_tool_distance_bwd<double>(L, h->d_col_off, (const double*)state, pose,
+                                                              (const double*)g_out, (double*)g_state, g_pose)
+                      : mpm::launch_tool_distance_bwd<float>(L, h->d_col_off, (const float*)state, pose,
+                                                             (const float*)g_out, (float*)g_state, g_pose);
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_tool_distance_bwd");
+}
+
 int mpm_status(MpmHandle* h, uint32_t* status, int32_t clear, void* stream) {
   if (!h || !status) return fail(h, MPM_E_INVALID, "mpm_status: NULL argument");
   MPM_TRY(check_device(h));
@@ -479,5 +553,48 @@ int mpm_last_error(MpmHandle* h, char* buf, size_t len) {
 }
 
 int64_t mpm_launch_count(MpmHandle* h) { return h ? h->launches : 0; }
+
+int mpm_profile_enable(MpmHandle* h, int32_t enable) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_profile_enable: NULL handle");
+  MPM_TRY(check_device(h));
+  const int kPairs = 1 << 16;
+  if (enable && h->events.empty()) {
+    h->events.resize(2 * kPairs);
+    for (auto& e : h->events) {
+      cudaError_t err = cudaEventCreate(&e);
+      if (err != cudaSuccess) return cuda_fail(h, err, "mpm_profile_enable: cudaEventCreate");
+    }
+    h->recs.resize(kPairs);
+  }
+  h->prof.on = enable != 0;
+  h->prof.pool = h->events.data();
+  h->prof.pool_cap = (int)h->events.size();
+  h->prof.recs = h->recs.data();
+  h->prof.cap = (int)h->recs.size();
+  return MPM_OK;
+}
+
+int mpm_profile_read(MpmHandle* h, double* ms, int64_t* count) {
+  if (!h || !ms || !count) return fail(h, MPM_E_INVALID, "mpm_profile_read: NULL argument");
+  MPM_TRY(check_device(h));
+  for (int k = 0; k < MPM_K_COUNT; ++k) {
+    ms[k] = 0.0;
+    count[k] = 0;
+  }
+  for (int i = 0; i < h->prof.n; ++i) {
+    const mpm::Profiler::Rec& r = h->prof.recs[i];
+    cudaError_t e = cudaEventSynchronize(r.b);
+    float t = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, r.a, r.b);
+    if (e != cudaSuccess) return cuda_fail(h, e, "mpm_profile_read");
+    if (r.kind >= 0 && r.kind < MPM_K_COUNT) {
+      ms[r.kind] += t;
+      count[r.kind] += 1;
+    }
+  }
+  h->prof.n = 0;
+  h->prof.pool_n = 0;
+  return MPM_OK;
+}
 
 }  // extern "C"

@@ -42,52 +42,40 @@ cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const d
   const int64_t nodes = (int64_t)c.n_scenes * c.G;
   Node<T>* gin = (Node<T>*)L.grid_a;
   Node<T>* gout = (Node<T>*)L.grid_b;
-  cudaError_t e = cudaMemsetAsync(gin, 0, nodes * sizeof(Node<T>), L.stream);
-  if (e != cudaSuccess) return e;
-  if (c.n_particles > 0) {
-    k_p2g<T, S><<<blocks_for(c.n_particles, 128), 128, 0, L.stream>>>(c, st0, st1, L.pscene, gin);
-    ++*L.launches;
-  }
-  k_grid_op<T><<<(unsigned)(nodes / 128), 128, 0, L.stream>>>(c, gin, gout, L.tools, L.tool_off, pose_f, pose_f1);
-  ++*L.launches;
-  if (c.n_particles > 0) {
-    k_g2p<T><<<blocks_for(c.n_particles, 128), 128, 0, L.stream>>>(c, st0, st1, L.pscene, gout);
-    ++*L.launches;
-  }
+  MPM_MEMSET(L, gin, nodes * sizeof(Node<T>));
+  if (c.n_particles > 0)
+    MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S>), blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gin);
+  MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, (unsigned)(nodes / 128), 128, c, gin, gout, L.tools, L.tool_off,
+             pose_f, pose_f1);
+  if (c.n_particles > 0)
+    MPM_LAUNCH(L, MPM_K_G2P, k_g2p<T>, blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gout);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_grid_mass(const LaunchCtx& L, const T* st, T* gm) {
   Consts<T> c = make_consts<T>(L);
-  cudaError_t e = cudaMemsetAsync(gm, 0, (int64_t)c.n_scenes * c.G * sizeof(T), L.stream);
-  if (e != cudaSuccess) return e;
-  if (c.n_particles > 0) {
-    k_grid_mass<T><<<blocks_for(c.n_particles, 128), 128, 0, L.stream>>>(c, st, L.pscene, gm);
-    ++*L.launches;
-  }
+  MPM_MEMSET(L, gm, (int64_t)c.n_scenes * c.G * sizeof(T));
+  if (c.n_particles > 0)
+    MPM_LAUNCH(L, MPM_K_OTHER, k_grid_mass<T>, blocks_for(c.n_particles, 128), 128, c, st, L.pscene, gm);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_grid_mass_bwd(const LaunchCtx& L, const T* st, const T* ggm, T* gst) {
   Consts<T> c = make_consts<T>(L);
-  if (c.n_particles > 0) {
-    k_grid_mass_adj<T><<<blocks_for(c.n_particles, 128), 128, 0, L.stream>>>(c, st, L.pscene, ggm, gst);
-    ++*L.launches;
-  }
+  if (c.n_particles > 0)
+    MPM_LAUNCH(L, MPM_K_OTHER, k_grid_mass_adj<T>, blocks_for(c.n_particles, 128), 128, c, st, L.pscene, ggm, gst);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_density_l1(const LaunchCtx& L, const T* gm, const T* tgt, double weight, double* loss, T* ggm) {
   const int S = L.p->n_scenes;
-  cudaError_t e = cudaMemsetAsync(loss, 0, S * sizeof(double), L.stream);
-  if (e != cudaSuccess) return e;
+  MPM_MEMSET(L, loss, S * sizeof(double));
   int bps = (int)((L.G + 256 * 8 - 1) / (256 * 8));
   if (bps < 1) bps = 1;
-  k_density_l1<T><<<(unsigned)(S * bps), 256, 0, L.stream>>>(L.G, gm, tgt, weight, loss, ggm, bps);
-  ++*L.launches;
+  MPM_LAUNCH(L, MPM_K_OTHER, k_density_l1<T>, (unsigned)(S * bps), 256, L.G, gm, tgt, weight, loss, ggm, bps);
   return cudaGetLastError();
 }
 
@@ -127,17 +115,61 @@ template <typename T>
 cudaError_t launch_soft_contact(const LaunchCtx& L, int n_tools, const T* st, const double* pose, double* sums,
                                 double* min_dist) {
   Consts<T> c = make_consts<T>(L);
-  cudaError_t e = cudaMemsetAsync(sums, 0, 2 * n_tools * sizeof(double), L.stream);
-  if (e != cudaSuccess) return e;
-  if (c.n_particles > 0) {
-    k_contact_sums<T><<<blocks_for(c.n_particles, 128), 128, 0, L.stream>>>(c, st, L.pscene, L.tools, L.tool_off,
-                                                                              pose, sums);
-    ++*L.launches;
-  }
-  k_contact_finish<<<blocks_for(n_tools, 64), 64, 0, L.stream>>>(n_tools, sums, min_dist);
-  ++*L.launches;
+  MPM_MEMSET(L, sums, 2 * n_tools * sizeof(double));
+  if (c.n_particles > 0)
+    MPM_LAUNCH(L, MPM_K_OTHER, k_contact_sums<T>, blocks_for(c.n_particles, 128), 128, c, st, L.pscene, L.tools,
+               L.tool_off, pose, sums);
+  MPM_LAUNCH(L, MPM_K_OTHER, k_contact_finish, blocks_for(n_tools, 64), 64, n_tools, sums, min_dist);
   return cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------
+// per-particle tool distances (function.py:79-89)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128) k_tool_distance(Consts<T> c, const T* __restrict__ st,
+                                                       const int* __restrict__ pscene,
+                                                       const MpmToolDesc* __restrict__ tools,
+                                                       const int* __restrict__ tool_off,
+                                                       const int* __restrict__ col_off,
+                                                       const double* __restrict__ pose, T* __restrict__ out) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= c.n_particles) return;
+  int sc = pscene[p];
+  T x[3];
+  load_row(st, c.ld, p, 0, 3, x);
+  for (int t = tool_off[sc]; t < tool_off[sc + 1]; ++t) {
+    Tool<T> tl;
+    Pose<T> P;
+    to_tool(tools[t], tl);
+    to_pose(pose + 8 * t, P);
+    const int col = col_off[t];
+    if (tl.type == TOOL_GRIPPER) {
+      T fa[3], fb[3];
+      finger_pos(P, T(-1), fa);
+      finger_pos(P, T(1), fb);
+      out[(int64_t)col * c.ld + p] = shape_sdf(tl, fa, P.rot, x);
+      out[(int64_t)(col + 1) * c.ld + p] = shape_sdf(tl, fb, P.rot, x);
+    } else {
+      out[(int64_t)col * c.ld + p] = tool_sdf(tl, P, x);
+    }
+  }
+}
+
+template <typename T>
+cudaError_t launch_tool_distance(const LaunchCtx& L, const int* col_off, int n_cols, const T* st, const double* pose,
+                                 T* out) {
+  Consts<T> c = make_consts<T>(L);
+  MPM_MEMSET(L, out, (int64_t)n_cols * c.ld * sizeof(T));
+  if (c.n_particles > 0)
+    MPM_LAUNCH(L, MPM_K_OTHER, k_tool_distance<T>, blocks_for(c.n_particles, 128), 128, c, st, L.pscene, L.tools,
+               L.tool_off, col_off, pose, out);
+  return cudaGetLastError();
+}
+template cudaError_t launch_tool_distance<float>(const LaunchCtx&, const int*, int, const float*, const double*,
+                                                 float*);
+template cudaError_t launch_tool_distance<double>(const LaunchCtx&, const int*, int, const double*, const double*,
+                                                  double*);
 
 #define MPM_INST_FWD(T, S) \
   template cudaError_t launch_substep_fwd<T, S>(const LaunchCtx&, const T*, T*, const double*, const double*);

@@ -8,6 +8,22 @@
 
 namespace mpm {
 
+// Optional per-kernel CUDA-event timing (mpm_profile_enable).
+struct Profiler {
+  struct Rec {
+    int kind;
+    cudaEvent_t a, b;
+  };
+  bool on = false;
+  Rec* recs = nullptr;
+  int n = 0, cap = 0;
+  cudaEvent_t* pool = nullptr;
+  int pool_n = 0, pool_cap = 0;
+};
+// bracket a launch: begin() before, end() after (no-ops when profiling is off)
+int prof_begin(Profiler* P, cudaStream_t s);
+void prof_end(Profiler* P, int slot, int kind, cudaStream_t s);
+
 struct LaunchCtx {
   const MpmParams* p;
   int64_t G;                   // n_grid^3
@@ -21,7 +37,24 @@ struct LaunchCtx {
   void* grid_d;
   cudaStream_t stream;
   int64_t* launches;           // launch counter
+  Profiler* prof;              // may be null
 };
+
+// launch helper: counts and (optionally) times one kernel launch
+#define MPM_LAUNCH(L, KIND, KERNEL, GRID, BLOCK, ...)                 \
+  do {                                                                 \
+    int _slot = prof_begin((L).prof, (L).stream);                      \
+    KERNEL<<<(GRID), (BLOCK), 0, (L).stream>>>(__VA_ARGS__);           \
+    prof_end((L).prof, _slot, (KIND), (L).stream);                     \
+    ++*(L).launches;                                                   \
+  } while (0)
+#define MPM_MEMSET(L, PTR, BYTES)                                      \
+  do {                                                                 \
+    int _slot = prof_begin((L).prof, (L).stream);                      \
+    cudaError_t _e = cudaMemsetAsync((PTR), 0, (BYTES), (L).stream);   \
+    prof_end((L).prof, _slot, MPM_K_CLEAR, (L).stream);                \
+    if (_e != cudaSuccess) return _e;                                  \
+  } while (0)
 
 template <typename T, typename S>
 cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const double* pose_f,
@@ -38,6 +71,12 @@ cudaError_t launch_density_l1(const LaunchCtx& L, const T* gm, const T* tgt, dou
 template <typename T>
 cudaError_t launch_soft_contact(const LaunchCtx& L, int n_tools, const T* st, const double* pose, double* sums,
                                 double* min_dist);
+template <typename T>
+cudaError_t launch_tool_distance(const LaunchCtx& L, const int* col_off, int n_cols, const T* st, const double* pose,
+                                 T* out);
+template <typename T>
+cudaError_t launch_tool_distance_bwd(const LaunchCtx& L, const int* col_off, const T* st, const double* pose,
+                                     const T* g_out, T* gst, double* g_pose);
 template <typename T>
 cudaError_t launch_soft_contact_bwd(const LaunchCtx& L, int n_tools, const T* st, const double* pose,
                                     const double* sums, const double* g_min, T* gst, double* g_pose);

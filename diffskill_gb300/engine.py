@@ -206,6 +206,22 @@ class MpmEngine:
         _lib.check(self.lib.mpm_soft_contact_bwd(self.h, _ptr(st), _ptr(pose), _ptr(sums), _ptr(g_md), _ptr(g_st),
                                                  _ptr(g_pose), _stream()), self.h, "mpm_soft_contact_bwd")
 
+    @property
+    def n_dist_cols(self) -> int:
+        return int(self.lib.mpm_tool_distance_cols(self.h))
+
+    def tool_distance(self, st, pose, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """[n_cols, ld] per-particle tool SDFs (Gripper: two finger columns)."""
+        if out is None:
+            out = torch.empty((max(self.n_dist_cols, 1), self.ld), dtype=self.dtype, device=self.device)
+        _lib.check(self.lib.mpm_tool_distance(self.h, _ptr(st), _ptr(pose), _ptr(out), _stream()), self.h,
+                   "mpm_tool_distance")
+        return out
+
+    def tool_distance_bwd(self, st, pose, g_out, g_st, g_pose) -> None:
+        _lib.check(self.lib.mpm_tool_distance_bwd(self.h, _ptr(st), _ptr(pose), _ptr(g_out), _ptr(g_st),
+                                                  _ptr(g_pose), _stream()), self.h, "mpm_tool_distance_bwd")
+
     def status(self, clear: bool = True) -> int:
         v = ctypes.c_uint32(0)
         _lib.check(self.lib.mpm_status(self.h, ctypes.byref(v), int(clear), _stream()), self.h, "mpm_status")
@@ -221,6 +237,18 @@ class MpmEngine:
     @property
     def launches(self) -> int:
         return int(self.lib.mpm_launch_count(self.h))
+
+    def profile(self, enable: bool) -> None:
+        """Bracket every kernel with CUDA events (not inside graph capture)."""
+        _lib.check(self.lib.mpm_profile_enable(self.h, int(enable)), self.h, "mpm_profile_enable")
+
+    def profile_read(self) -> dict:
+        """{kind: (total device ms, launches)} since the last read."""
+        n = len(_lib.KERNEL_KINDS)
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_int64 * n)()
+        _lib.check(self.lib.mpm_profile_read(self.h, ms, cnt), self.h, "mpm_profile_read")
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(_lib.KERNEL_KINDS)}
 
     # ------------------------------------------------------------- helpers
     def targets(self, grids: Sequence[np.ndarray]) -> torch.Tensor:
@@ -260,6 +288,10 @@ class Horizon:
         self.g = torch.zeros((2, N_ROWS, eng.ld), dtype=dt, device=dev)
         self.gm = torch.zeros((eng.S, eng.G), dtype=dt, device=dev)
         self.g_gm = torch.zeros_like(self.gm)
+        # contact-term tables (built once: no host->device copy inside a CUDA graph)
+        self.movable = torch.tensor([float(t.action.dim > 0) for t in eng.tool_cfgs] or [0.0],
+                                    dtype=torch.float64, device=dev)[:eng.T]
+        self.tool_scene = torch.tensor(eng.tool_scene or [0], dtype=torch.long, device=dev)[:eng.T]
 
     def bytes(self) -> int:
         return sum(t.numel() * t.element_size() for t in
@@ -302,10 +334,8 @@ class Horizon:
             self._loss_grad_ready = True
         if contact_weight and eng.T:
             md, sums = eng.soft_contact(final, self.pose[self.F])
-            movable = torch.tensor([float(t.action.dim > 0) for t in eng.tool_cfgs], dtype=torch.float64,
-                                   device=eng.device)
-            scene = torch.tensor(eng.tool_scene, device=eng.device)
-            loss = loss.index_add(0, scene, contact_weight * md * md * movable)
+            movable = self.movable
+            loss = loss.index_add(0, self.tool_scene, contact_weight * md * md * movable)
             if need_grad:
                 g_md = (2 * contact_weight * md * movable).contiguous()
                 eng.soft_contact_bwd(final, self.pose[self.F], sums, g_md, g_final, self.g_pose[self.F])

@@ -1,0 +1,116 @@
+"""Batched trajectory optimisation: forward, density loss, adjoint, Adam.
+
+One ``BatchedTrajectory.step()`` is one iteration of
+``Solver.solve_one_plan`` (plb/optimizer/solver.py:97-152) for every scene of
+the batch at once: reset to the initial state, run all actions forward,
+compute the per-scene loss, run the checkpointed adjoint, take an Adam step on
+the actions (torch.optim.Adam semantics, lr 0.01 default) and clip them to
+[-1, 1].  The whole step is capturable as one CUDA graph: no host sync, no
+allocation after the first call.
+"""
+from __future__ import annotations
+
+from typing import List, Optional, Sequence
+
+import torch
+
+from .engine import Horizon, MpmEngine
+from .scenes import Scene
+
+
+def _check_compatible(scenes: Sequence[Scene]) -> None:
+    s0 = scenes[0].sim
+    for sc in scenes[1:]:
+        s = sc.sim
+        same = (s.grid == s0.grid and s.step_dt == s0.step_dt and s.n_substeps == s0.n_substeps and s.E == s0.E
+                and s.nu == s0.nu and s.yield_stress == s0.yield_stress and tuple(s.gravity) == tuple(s0.gravity)
+                and s.ground_friction == s0.ground_friction and s.precision_code == s0.precision_code
+                and sc.n_actions == scenes[0].n_actions)
+        if not same:
+            raise ValueError("batched scenes must share grid, dt, substeps, material, precision and horizon")
+
+
+class BatchedTrajectory:
+    def __init__(self, scenes: Sequence[Scene], ckpt_every: Optional[int] = None, lr: float = 0.01,
+                 betas=(0.9, 0.999), eps: float = 1e-8, softness: float = 666.0):
+        scenes = list(scenes)
+        _check_compatible(scenes)
+        self.scenes = scenes
+        self.eng = MpmEngine(scenes[0].sim, [sc.tools for sc in scenes], [sc.n_particles for sc in scenes],
+                             softness=softness)
+        k = ckpt_every if ckpt_every else (scenes[0].checkpoint_every or scenes[0].sim.n_substeps)
+        self.hz = Horizon(self.eng, scenes[0].n_actions, ckpt_every=k)
+        eng = self.eng
+        self.state0 = eng.init_state([sc.x0 for sc in scenes])
+        self.targets = eng.targets([sc.target for sc in scenes])
+        self.actions = eng.expand_actions([sc.actions for sc in scenes])
+        mask = torch.zeros((1, max(eng.T, 1), 8), dtype=torch.float64, device=eng.device)
+        for t, cfg in enumerate(eng.tool_cfgs):
+            mask[0, t, :int(cfg.action.dim)] = 1
+        self.mask = mask
+        self.density_weight = scenes[0].density_weight
+        self.contact_weight = scenes[0].contact_weight
+        self.lr, self.betas, self.eps = lr, betas, eps
+        self.m = torch.zeros_like(self.actions)
+        self.v = torch.zeros_like(self.actions)
+        self.t = torch.zeros((), dtype=torch.float64, device=eng.device)
+        self._b = torch.tensor(list(betas), dtype=torch.float64, device=eng.device)
+        self.loss = torch.zeros(eng.S, dtype=torch.float64, device=eng.device)
+        self.grad = torch.zeros_like(self.actions)
+        self.graph: Optional[torch.cuda.CUDAGraph] = None
+
+    @property
+    def particle_substeps(self) -> int:
+        return self.eng.P * self.hz.F
+
+    def forward_backward(self) -> None:
+        hz = self.hz
+        hz.forward(self.state0, self.actions)
+        self.loss.copy_(hz.loss(self.targets, self.density_weight, self.contact_weight))
+        self.grad.copy_(hz.backward())
+
+    def adam(self) -> None:
+        """torch.optim.Adam update, then clamp to [-1, 1] and mask (solver.py:128-133)."""
+        b1, b2 = self.betas
+        g = self.grad * self.mask
+        self.t.add_(1)
+        self.m.mul_(b1).add_(g, alpha=1 - b1)
+        self.v.mul_(b2).addcmul_(g, g, value=1 - b2)
+        bc1 = 1 - torch.pow(self._b[0], self.t)
+        bc2 = 1 - torch.pow(self._b[1], self.t)
+        denom = (self.v / bc2).sqrt_().add_(self.eps)
+        self.actions.sub_(self.lr * (self.m / bc1) / denom)
+        self.actions.clamp_(-1, 1).mul_(self.mask)
+
+    def step(self) -> None:
+        """One optimisation iteration (replays the CUDA graph when captured)."""
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self.forward_backward()
+            self.adam()
+
+    def capture(self) -> None:
+        """Capture forward + backward + Adam of one iteration as a CUDA graph."""
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):  # warm allocations outside the capture
+            self.forward_backward()
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.forward_backward()
+            self.adam()
+        torch.cuda.synchronize()
+        self.graph = g
+
+    def reset_optimizer(self, actions: Optional[List] = None) -> None:
+        if actions is not None:
+            self.actions.copy_(self.eng.expand_actions(actions))
+        self.m.zero_()
+        self.v.zero_()
+        self.t.zero_()
+
+    def action_grads(self) -> List[torch.Tensor]:
+        return self.eng.collapse_action_grad(self.grad)

@@ -160,12 +160,44 @@ int mpm_soft_contact(MpmHandle* h, const void* state, const double* pose, double
 int mpm_soft_contact_bwd(MpmHandle* h, const void* state, const double* pose, const double* sums,
                          const double* g_min_dist, void* g_state, double* g_pose, void* stream);
 
+/* Per-particle tool distances (GradModel.compute_min_dist, function.py:79-89):
+ * column c of out (real[n_cols][ld], n_cols from mpm_tool_distance_cols) holds
+ * the SDF of the tool owning column c at every particle of that tool's scene
+ * (Gripper: two columns, finger -1 then finger +1, as sdf_2 of
+ * primitives.py:479-483), and 0 for particles of other scenes. */
+int mpm_tool_distance_cols(MpmHandle* h);
+int mpm_tool_distance(MpmHandle* h, const void* state, const double* pose, void* out, void* stream);
+/* Adjoint (compute_min_dist.grad, function.py:154-159): accumulates the x
+ * rows of g_state and g_pose (double[n_tools][8]) from g_out. */
+int mpm_tool_distance_bwd(MpmHandle* h, const void* state, const double* pose, const void* g_out, void* g_state,
+                          double* g_pose, void* stream);
+
 /* Reads the sticky device status word (synchronises the stream). */
 int mpm_status(MpmHandle* h, uint32_t* status, int32_t clear, void* stream);
 /* Copies the last error message of this handle (or of mpm_create if h is NULL). */
 int mpm_last_error(MpmHandle* h, char* buf, size_t len);
 /* Number of kernel launches issued through this handle since creation. */
 int64_t mpm_launch_count(MpmHandle* h);
+
+/* Kernel kinds reported by the profiler. */
+#define MPM_K_P2G 0          /* p2g writing F' (forward)           */
+#define MPM_K_P2G_RECOMP 1   /* p2g recomputing the grid (adjoint)  */
+#define MPM_K_GRID_OP 2
+#define MPM_K_G2P 3
+#define MPM_K_G2P_ADJ 4
+#define MPM_K_GRID_OP_ADJ 5
+#define MPM_K_P2G_ADJ 6
+#define MPM_K_CLEAR 7        /* grid clears (memset)               */
+#define MPM_K_OTHER 8        /* density, loss, contact, tools       */
+#define MPM_K_COUNT 9
+
+/* No counterpart in the reference (it has no profiler): when enabled, every
+ * kernel launched through the handle is bracketed by a CUDA event pair on its
+ * stream.  Not for use inside CUDA-graph capture. */
+int mpm_profile_enable(MpmHandle* h, int32_t enable);
+/* Synchronises, then writes per kind the summed device milliseconds and the
+ * launch counts since the last read (arrays of MPM_K_COUNT), and resets. */
+int mpm_profile_read(MpmHandle* h, double* ms, int64_t* count);
 
 #ifdef __cplusplus
 }

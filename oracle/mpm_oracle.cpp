@@ -1167,6 +1167,37 @@ void oracle_tool_sdf_vjp(const OracleTool* tool, const double* pose, int64_t m, 
                          double* g_pts, double* g_pose) {
   for (int64_t i = 0; i < m; ++i) tool_sdf_vjp(*tool, pose, pts + 3 * i, g[i], g_pts + 3 * i, g_pose);
 }
+// per-point distance columns of one tool (GradModel.compute_min_dist,
+// function.py:79-89): Gripper -> two columns (sdf_2 with flag -1, +1,
+// primitives.py:479-483), other tools -> one column (sdf).  out: [m][ncol].
+int oracle_tool_distance_cols(const OracleTool* tool) { return tool->type == T_GRIPPER ? 2 : 1; }
+void oracle_tool_distance(const OracleTool* tool, const double* pose, int64_t m, const double* pts, double* out) {
+  const int nc = oracle_tool_distance_cols(tool);
+  for (int64_t i = 0; i < m; ++i) {
+    if (tool->type == T_GRIPPER) {
+      out[i * nc] = shape_sdf(*tool, K_BOX, finger_pose(pose, -1), pts + 3 * i);
+      out[i * nc + 1] = shape_sdf(*tool, K_BOX, finger_pose(pose, 1), pts + 3 * i);
+    } else {
+      out[i * nc] = tool_sdf(*tool, pose, pts + 3 * i);
+    }
+  }
+}
+void oracle_tool_distance_vjp(const OracleTool* tool, const double* pose, int64_t m, const double* pts,
+                              const double* g, double* g_pts, double* g_pose) {
+  const int nc = oracle_tool_distance_cols(tool);
+  for (int64_t i = 0; i < m; ++i) {
+    if (tool->type == T_GRIPPER) {
+      for (int side = 0; side < 2; ++side) {
+        double flag = side == 0 ? -1.0 : 1.0;
+        PoseGrad gF;
+        shape_sdf_vjp(*tool, K_BOX, finger_pose(pose, flag), pts + 3 * i, g[i * nc + side], g_pts + 3 * i, &gF);
+        finger_pose_vjp(pose, flag, gF, g_pose);
+      }
+    } else {
+      tool_sdf_vjp(*tool, pose, pts + 3 * i, g[i * nc], g_pts + 3 * i, g_pose);
+    }
+  }
+}
 // one tool's collide at m points (tests)
 void oracle_tool_collide(const OracleTool* tool, const double* pose0, const double* pose1, double dt, int64_t m,
                          const double* pts, const double* vin, double* vout) {

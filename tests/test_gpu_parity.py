@@ -147,10 +147,13 @@ def test_checkpoint_recompute_equals_store_all(gpu_lib):
 
 
 def test_batched_scenes_equal_single_scenes(gpu_lib):
+    """Three scenes with different particle counts and tool sets in one launch
+    give the same loss and action gradients as three separate runs."""
     base = small_scene(n=1500, n_actions=1, substeps=20, precision="fp64")
     scs = [small_scene(n=1000 + 500 * i, n_actions=1, substeps=20, precision="fp64", seed=2000 + i)
            for i in range(3)]
-    tools = [[base.tools[0]], [all_tools()[2]], [all_tools()[0], all_tools()[4]]]
+    at = all_tools()
+    tools = [[at[1]], [at[2]], [at[0], at[4]]]  # every tool touches the dough
     for sc, tl in zip(scs, tools):
         sc.tools = tl
         sc.actions = np.random.default_rng(len(tl)).uniform(-1, 1, size=(1, sum(t.action.dim for t in tl)))
@@ -164,7 +167,9 @@ def test_batched_scenes_equal_single_scenes(gpu_lib):
         e1 = MpmEngine(sc.sim, [tools[i]], [sc.n_particles])
         l1, g1, _ = _traj(e1, sc, k=10)
         assert abs(float(loss[i]) - l1) <= 1e-12 * abs(l1)
-        assert rel_err(g[i].cpu().numpy(), g1) < 1e-9
+        gi = g[i].cpu().numpy()
+        assert np.abs(g1).max() > 1e-6  # the tools act on the dough
+        assert np.abs(gi - g1).max() <= 1e-9 * np.abs(g1).max(), (gi, g1)
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
