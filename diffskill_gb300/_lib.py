@@ -61,6 +61,8 @@ SIGNATURES = {
     "mpm_tool_distance_cols": (_i32, [_c_p]),
     "mpm_tool_distance": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_tool_distance_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
+    "mpm_substep_fwd_static": (_i32, [ctypes.POINTER(MpmParams), ctypes.POINTER(MpmToolDesc), _i32, _c_p, _c_p, _c_p,
+                                      _c_p, _c_p]),
     "mpm_status": (_i32, [_c_p, ctypes.POINTER(ctypes.c_uint32), _i32, _c_p]),
     "mpm_last_error": (_i32, [_c_p, ctypes.c_char_p, ctypes.c_size_t]),
     "mpm_launch_count": (_i64, [_c_p]),

@@ -34,6 +34,7 @@ struct MpmHandle {
 };
 
 namespace mpm {
+void record_global_error(const std::string& msg);
 int prof_begin(Profiler* P, cudaStream_t s) {
   if (!P || !P->on) return -1;
   if (P->pool_n + 2 > P->pool_cap) return -1;  // pool exhausted: drop this sample
@@ -64,6 +65,15 @@ int fail(MpmHandle* h, int code, const std::string& msg) {
   }
   return code;
 }
+}  // namespace
+
+void mpm::record_global_error(const std::string& msg) {
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_create_err = msg;
+}
+
+namespace {
+
 int cuda_fail(MpmHandle* h, cudaError_t e, const char* where) {
   return fail(h, MPM_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }

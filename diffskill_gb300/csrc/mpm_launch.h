@@ -4,9 +4,14 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "../../include/mpm_gb300.h"
 
 namespace mpm {
+
+// Stores the message returned by mpm_last_error(NULL, ...) (mpm_capi.cu).
+void record_global_error(const std::string& msg);
 
 // Optional per-kernel CUDA-event timing (mpm_profile_enable).
 struct Profiler {

@@ -172,6 +172,27 @@ int mpm_tool_distance(MpmHandle* h, const void* state, const double* pose, void*
 int mpm_tool_distance_bwd(MpmHandle* h, const void* state, const double* pose, const void* g_out, void* g_state,
                           double* g_pose, void* stream);
 
+/* No counterpart in the reference.  One forward substep (as mpm_substep_fwd)
+ * of a single scene that allocates nothing, for callers that cannot call
+ * cudaMalloc: code stepping the scene from inside another framework's GPU
+ * memory pool (which may hold nearly all of HBM and must not be bypassed),
+ * or latency-bound loops that cannot afford the device-wide synchronisation
+ * of cudaMalloc/cudaFree.  No handle: params (n_scenes = 1) and the host tool
+ * table are passed per call; the caller still owns state_f, state_f1, pose_f
+ * and pose_f1.  Grid scratch, tool table and status word live in one
+ * file-scope static device array of 20 MiB + 8 KiB, held by every GPU that
+ * loads the library until the process exits.  Limits: n_particles <= 2^20;
+ * two grids of n_grid^3 nodes within 16 MiB (n_grid <= 80 in FP32, <= 64 in
+ * FP64); at most 8 tools.  Larger sizes return MPM_E_INVALID; the message is
+ * read with mpm_last_error(NULL, ...).  The first call on a device performs
+ * set-up (cudaGetSymbolAddress on that device and zeroing of the array's
+ * scene-index region); make that first call before any stream capture.  All
+ * calls share the array: calls whose kernels overlap on the GPU race, so
+ * serialise them.  The device status word is cleared per call and not
+ * reported. */
+int mpm_substep_fwd_static(const MpmParams* params, const MpmToolDesc* tools, int32_t n_tools, const void* state_f,
+                           void* state_f1, const double* pose_f, const double* pose_f1, void* stream);
+
 /* Reads the sticky device status word (synchronises the stream). */
 int mpm_status(MpmHandle* h, uint32_t* status, int32_t clear, void* stream);
 /* Copies the last error message of this handle (or of mpm_create if h is NULL). */
