@@ -18,6 +18,7 @@ host cores instead.
 from __future__ import annotations
 
 import argparse
+import copy
 import json
 import os
 import subprocess
@@ -148,6 +149,23 @@ ALGO_WORDS = {"p2g": ("particle", 33), "p2g_recompute": ("particle", 24), "g2p":
               "grid_op_adj": ("node", 12)}
 
 
+def active_blocks(xs, n_grid: int) -> int:
+    """Number of 4^3-node grid blocks the particle stencils touch (summed over
+    scenes), the unit count of the sparse grid kernels."""
+    nb = n_grid // 4
+    tot = 0
+    for x in xs:
+        base = np.clip((np.asarray(x) * n_grid - 0.5).astype(np.int64), 0, n_grid - 3)
+        keys = set()
+        for o in (0, 2):
+            for q in (0, 2):
+                for r in (0, 2):
+                    b = (base + np.array([o, q, r])) >> 2
+                    keys.update(((b[:, 0] * nb + b[:, 1]) * nb + b[:, 2]).tolist())
+        tot += len(keys)
+    return tot
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -265,7 +283,10 @@ def run_ours(args, rank, world, dist):
         return None
 
     w = 4 if eng.dtype == torch.float32 else 8
-    units = {"particle": eng.P, "node": eng.S * eng.G}
+    fin = bt.hz.final[0:3, :eng.P].double().cpu().numpy().T
+    xs = [fin[int(eng.offsets[i]):int(eng.offsets[i + 1])] for i in range(eng.S)]
+    nblk = active_blocks(xs, eng.n_grid)
+    units = {"particle": eng.P, "node": nblk * 64}
     kern = {}
     for kname, (tot_ms, cnt) in prof.items():
         if cnt == 0:
@@ -294,6 +315,7 @@ def run_ours(args, rank, world, dist):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; reference datasets not shipped)",
         "config": dict(desc, particles_per_rank=eng.P, substeps_per_step=bt.hz.F, checkpoint_every=k,
+                       active_grid_blocks_final=nblk, grid_blocks_total=eng.S * eng.G // 64,
                        cuda_graph=use_graph, parallelism=f"scene-sharded x{world}" if world > 1 else "single GPU",
                        l2="working set per step far above the 129 MB L2 (state frames + 4 grids)"),
         "e2e": {"value": tot_ps / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d * world,
@@ -330,25 +352,42 @@ def extras(args, scs, grad0, bt):
                                      "all frames stored, eager launches",
                          "batched_fp32_over_plain_fp64": None}
     del p64
-    # FP32 action gradients vs the FP64 GPU path on the same scenes (first 4)
-    sub = scs[:4]
+    # FP32 action gradients vs the FP64 GPU path on the same scenes (first 16, checkpointed)
+    sub = [copy.deepcopy(s) for s in scs[:16]]
     for s in sub:
         s.sim.precision = "fp64"
-    try:
-        r64 = BatchedTrajectory(sub, ckpt_every=bt.hz.k)
-        r64.forward_backward()
-        torch.cuda.synchronize()
-        g64 = [g.detach().cpu().numpy() for g in r64.action_grads()]
-        errs = [float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30)) for a, b in zip(grad0, g64)]
-        res["accuracy"] = {"action_grad_rel_err_fp32_vs_fp64": max(errs), "per_scene": errs,
-                           "scenes_checked": len(sub), "norm": "max|g32-g64|/max|g64| per scene"}
-        del r64
-    finally:
-        for s in sub:
-            s.sim.precision = "fp32"
+    r64 = BatchedTrajectory(sub, ckpt_every=10)
+    r64.forward_backward()
+    torch.cuda.synchronize()
+    g64 = [g.detach().cpu().numpy() for g in r64.action_grads()]
+    del r64
+    torch.cuda.empty_cache()
+    res["accuracy"] = grad_errors(grad0[:len(g64)], g64)
+    res["accuracy"]["scenes_checked"] = len(g64)
     # CPU baseline: the FP64 oracle on the host cores, bounded sample of the same workload
     res["cpu_baseline"] = cpu_baseline(scs[0], target_s=12.0)
     return res
+
+
+def grad_errors(g32, g64):
+    """Per-scene relative action-gradient errors, L2 and max norms.  Scenes whose
+    FP64 gradient is below 1e-6 of the median norm (tools not acting on the
+    dough) have no defined relative error and are listed as excluded."""
+    norms = [float(np.linalg.norm(b)) for b in g64]
+    med = float(np.median(norms)) if norms else 0.0
+    l2, mx, excl = [], [], []
+    for i, (a, b) in enumerate(zip(g32, g64)):
+        if norms[i] <= 1e-6 * med:
+            excl.append(i)
+            continue
+        l2.append(float(np.linalg.norm(a - b) / norms[i]))
+        mx.append(float(np.abs(a - b).max() / np.abs(b).max()))
+    return {"action_grad_rel_err_l2_median": float(np.median(l2)) if l2 else None,
+            "action_grad_rel_err_l2_max": max(l2) if l2 else None,
+            "action_grad_rel_err_maxnorm_median": float(np.median(mx)) if mx else None,
+            "action_grad_rel_err_maxnorm_max": max(mx) if mx else None,
+            "scenes_within_1e-3_l2": int(sum(e <= 1e-3 for e in l2)), "scenes_compared": len(l2),
+            "excluded_zero_gradient": excl, "reference": "FP64 GPU path on the same scenes and actions"}
 
 
 def cpu_baseline(sc, target_s: float = 12.0, threads: int = 0):

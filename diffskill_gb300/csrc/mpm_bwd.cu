@@ -7,6 +7,9 @@ namespace mpm {
 
 template <typename T>
 Consts<T> make_consts(const LaunchCtx& L);  // mpm_fwd.cu
+template <typename T>
+cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* b);
+unsigned grid_blocks_launch(const LaunchCtx& L, int64_t total_blocks);
 
 static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
@@ -14,22 +17,23 @@ template <typename T, typename S>
 cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* g1, T* g0, const double* pose_f,
                                const double* pose_f1, double* g_pose_f, double* g_pose_f1) {
   Consts<T> c = make_consts<T>(L);
-  const int64_t nodes = (int64_t)c.n_scenes * c.G;
   Node<T>* gin = (Node<T>*)L.grid_a;
   Node<T>* gout = (Node<T>*)L.grid_b;
   Node<T>* g_gin = (Node<T>*)L.grid_c;
   Node<T>* g_gout = (Node<T>*)L.grid_d;
+  const int* counter = reinterpret_cast<const int*>(L.blockbuf);
   const unsigned pb = blocks_for(c.n_particles, 128);
+  const unsigned gb = grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3);
   // recompute the grid of this substep (substep_grad, mpm_simulator.py:327-333)
-  MPM_MEMSET(L, gin, nodes * sizeof(Node<T>));
+  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, g_gout);
+  if (e != cudaSuccess) return e;
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_P2G_RECOMP, (k_p2g<T, S>), pb, 128, c, st0, (T*)nullptr, L.pscene, gin);
-  MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, (unsigned)(nodes / 128), 128, c, gin, gout, L.tools, L.tool_off,
-             pose_f, pose_f1);
-  MPM_MEMSET(L, g_gout, nodes * sizeof(Node<T>));
+  MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, gb, 64, c, L.active, counter, gin, gout, L.tools, L.tool_off, pose_f,
+             pose_f1);
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_G2P_ADJ, k_g2p_adj<T>, pb, 128, c, st0, g1, g0, L.pscene, gout, g_gout);
-  MPM_LAUNCH(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, (unsigned)(nodes / 128), 128, c, gin, g_gout, g_gin, L.tools,
+  MPM_LAUNCH(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, gb, 64, c, L.active, counter, gin, g_gout, g_gin, L.tools,
              L.tool_off, pose_f, pose_f1, g_pose_f, g_pose_f1);
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_P2G_ADJ, (k_p2g_adj<T, S>), pb, 128, c, st0, g1, g0, L.pscene, g_gin);

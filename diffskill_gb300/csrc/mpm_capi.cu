@@ -26,6 +26,9 @@ struct MpmHandle {
   std::vector<MpmToolDesc> h_tools;
   unsigned int* d_status = nullptr;
   void* grid[4] = {nullptr, nullptr, nullptr, nullptr};
+  unsigned char* d_blockbuf = nullptr;
+  int* d_active = nullptr;
+  int sm_count = 1;
   std::string err;
   int64_t launches = 0;
   mpm::Profiler prof;
@@ -91,6 +94,9 @@ mpm::LaunchCtx ctx(MpmHandle* h, void* stream) {
   L.grid_b = h->grid[1];
   L.grid_c = h->grid[2];
   L.grid_d = h->grid[3];
+  L.blockbuf = h->d_blockbuf;
+  L.active = h->d_active;
+  L.sm_count = h->sm_count;
   L.stream = (cudaStream_t)stream;
   L.launches = &h->launches;
   L.prof = &h->prof;
@@ -252,6 +258,12 @@ int mpm_create(const MpmParams* params, const int64_t* scene_offsets, MpmHandle*
   ok = ok && cudaMalloc(&h->d_tool_off, toff.size() * sizeof(int)) == cudaSuccess;
   ok = ok && cudaMalloc(&h->d_status, sizeof(unsigned int)) == cudaSuccess;
   for (int i = 0; i < 4 && ok; ++i) ok = cudaMalloc(&h->grid[i], gbytes) == cudaSuccess;
+  const int64_t nb = p.n_grid / 4;
+  const int64_t nblocks = (int64_t)p.n_scenes * nb * nb * nb;
+  ok = ok && cudaMalloc(&h->d_blockbuf, mpm::blockbuf_bytes(p.n_scenes, p.n_grid)) == cudaSuccess;
+  ok = ok && cudaMalloc(&h->d_active, nblocks * sizeof(int)) == cudaSuccess;
+  if (ok) cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
+  if (h->sm_count < 1) h->sm_count = 1;
   if (!ok) {
     cudaGetLastError();
     mpm_destroy(h);
@@ -277,6 +289,8 @@ int mpm_destroy(MpmHandle* h) {
   cudaFree(h->d_tools);
   cudaFree(h->d_status);
   for (int i = 0; i < 4; ++i) cudaFree(h->grid[i]);
+  cudaFree(h->d_blockbuf);
+  cudaFree(h->d_active);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
   delete h;
   return MPM_OK;

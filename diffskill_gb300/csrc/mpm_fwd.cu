@@ -14,6 +14,8 @@ Consts<T> make_consts(const LaunchCtx& L) {
   c.n_particles = p.n_particles;
   c.ld = p.ld;
   c.G = L.G;
+  c.nb = p.n_grid / 4;
+  c.NB3 = (int64_t)c.nb * c.nb * c.nb;
   c.dx = T(p.dx);
   c.inv_dx = T(p.inv_dx);
   c.dt = T(p.dt);
@@ -35,18 +37,44 @@ template Consts<double> make_consts<double>(const LaunchCtx&);
 
 static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+// Active blocks of frame st: clear flags, mark, compact, then zero the listed
+// blocks of grid a (and b if given).  Leaves the list in L.active and its
+// length at L.blockbuf[0..3].
+template <typename T>
+cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* b) {
+  const int64_t total = (int64_t)c.n_scenes * c.NB3;
+  int* counter = reinterpret_cast<int*>(L.blockbuf);
+  unsigned char* flags = L.blockbuf + 16;
+  MPM_MEMSET(L, L.blockbuf, blockbuf_bytes(c.n_scenes, c.n_grid));
+  if (c.n_particles > 0)
+    MPM_LAUNCH(L, MPM_K_CLEAR, k_mark_blocks<T>, blocks_for(c.n_particles, 256), 256, c, st, L.pscene, flags);
+  MPM_LAUNCH(L, MPM_K_CLEAR, k_compact_blocks, blocks_for(total, 256), 256, flags, total, L.active, counter);
+  MPM_LAUNCH(L, MPM_K_CLEAR, k_clear_blocks<T>, (unsigned)(L.sm_count * 8), 256, L.active, counter, a, b);
+  return cudaGetLastError();
+}
+template cudaError_t prepare_blocks<float>(const LaunchCtx&, const Consts<float>&, const float*, Node<float>*,
+                                           Node<float>*);
+template cudaError_t prepare_blocks<double>(const LaunchCtx&, const Consts<double>&, const double*, Node<double>*,
+                                            Node<double>*);
+
+unsigned grid_blocks_launch(const LaunchCtx& L, int64_t total_blocks) {
+  int64_t g = (int64_t)L.sm_count * 16;
+  return (unsigned)(g < total_blocks ? g : (total_blocks > 0 ? total_blocks : 1));
+}
+
 template <typename T, typename S>
 cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const double* pose_f,
                                const double* pose_f1) {
   Consts<T> c = make_consts<T>(L);
-  const int64_t nodes = (int64_t)c.n_scenes * c.G;
   Node<T>* gin = (Node<T>*)L.grid_a;
   Node<T>* gout = (Node<T>*)L.grid_b;
-  MPM_MEMSET(L, gin, nodes * sizeof(Node<T>));
+  const int* counter = reinterpret_cast<const int*>(L.blockbuf);
+  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, (Node<T>*)nullptr);
+  if (e != cudaSuccess) return e;
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S>), blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gin);
-  MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, (unsigned)(nodes / 128), 128, c, gin, gout, L.tools, L.tool_off,
-             pose_f, pose_f1);
+  MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3), 64, c, L.active,
+             counter, gin, gout, L.tools, L.tool_off, pose_f, pose_f1);
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_G2P, k_g2p<T>, blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gout);
   return cudaGetLastError();

@@ -13,6 +13,15 @@
 //   k_p2g_adj      p2g.grad + svd_grad + compute_F_tmp.grad (gather)
 //
 // Particle state is component-major: row k of a frame is st[k*ld + p].
+//
+// Sparse grid: the scratch grids of a substep are stored block-contiguous
+// (blocks of 4x4x4 nodes, 64 nodes = 1 KiB in FP32 per block).  Each substep
+// marks the blocks that particle stencils touch (k_mark_blocks), compacts them
+// into a device-side list (k_compact_blocks), clears only those
+// (k_clear_blocks), and runs grid_op / grid_op.grad over that list with
+// grid-stride loops (no host round trip; capturable in a CUDA graph).  Nodes
+// outside the list hold no mass, so grid_op leaves them at zero exactly as the
+// dense reference does; g2p and p2g.grad only read nodes inside the list.
 #pragma once
 #include "../../include/mpm_gb300.h"
 #include "mpm_math.cuh"
@@ -33,7 +42,9 @@ struct Consts {
   int n_scenes;
   int64_t n_particles;
   int64_t ld;
-  int64_t G;  // n_grid^3
+  int64_t G;    // n_grid^3
+  int nb;       // blocks per axis (n_grid / 4)
+  int64_t NB3;  // blocks per scene
   T dx, inv_dx, dt, p_mass, p_vol;
   T mu, lam, yield_stress;
   T ks;      // -dt * p_vol * 4 * inv_dx^2 (mpm_simulator.py:214)
@@ -93,6 +104,84 @@ MPM_DI T dweight(const Stencil<T>& s, int k, int d) {
 template <typename T>
 MPM_DI int64_t node_of(const Consts<T>& c, const Stencil<T>& s, int ox, int oy, int oz) {
   return ((int64_t)(s.base[0] + ox) * c.n_grid + (s.base[1] + oy)) * c.n_grid + (s.base[2] + oz);
+}
+
+// Offsets, within one scene's block-contiguous grid, of the stencil nodes
+// base+o per axis: node (i,j,k) -> ((bi*nb + bj)*nb + bk)*64 + (li*16 + lj*4 + lk)
+struct StencilAddr {
+  int ax[3], ay[3], az[3];
+  MPM_DI int at(int ox, int oy, int oz) const { return ax[ox] + ay[oy] + az[oz]; }
+};
+template <typename T>
+MPM_DI StencilAddr stencil_addr(const Consts<T>& c, const Stencil<T>& s) {
+  StencilAddr a;
+  const int nb = c.nb;
+#pragma unroll
+  for (int o = 0; o < 3; ++o) {
+    const int i = s.base[0] + o, j = s.base[1] + o, k = s.base[2] + o;
+    a.ax[o] = ((i >> 2) * nb * nb << 6) + ((i & 3) << 4);
+    a.ay[o] = ((j >> 2) * nb << 6) + ((j & 3) << 2);
+    a.az[o] = ((k >> 2) << 6) + (k & 3);
+  }
+  return a;
+}
+// grid coordinates of node l (0..63) of global block gb (= scene*NB3 + local block)
+template <typename T>
+MPM_DI int block_node(const Consts<T>& c, int64_t gb, int l, int* I) {
+  const int scene = (int)(gb / c.NB3);
+  const int64_t lb = gb - (int64_t)scene * c.NB3;
+  const int nb = c.nb;
+  I[0] = (int)(lb / ((int64_t)nb * nb)) * 4 + (l >> 4);
+  I[1] = (int)((lb / nb) % nb) * 4 + ((l >> 2) & 3);
+  I[2] = (int)(lb % nb) * 4 + (l & 3);
+  return scene;
+}
+
+// Warp-level segmented reduction of the scatter.  Particles are sorted by
+// base cell, so lanes with equal key (scene, base cell) are contiguous and
+// scatter into the same 27 nodes: an inclusive segmented scan leaves each
+// segment's sum in its last lane, which alone issues the atomic.  Lanes with a
+// unique key (out of range, out of grid) form single-lane segments.
+struct WarpSeg {
+  int start;  // first lane of this lane's segment
+  bool tail;  // this lane ends its segment
+  int steps;  // doubling steps that cover the longest segment (warp-uniform)
+};
+MPM_DI WarpSeg warp_segments(long long key) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const long long prev = __shfl_up_sync(full, key, 1);
+  const bool head = lane == 0 || prev != key;
+  const unsigned heads = __ballot_sync(full, head);
+  WarpSeg g;
+  g.start = 31 - __clz(heads & (full >> (31 - lane)));
+  g.tail = lane == 31 || ((heads >> (lane + 1)) & 1u);
+  const unsigned run = __reduce_max_sync(full, (unsigned)(lane - g.start + 1));
+  g.steps = run <= 1 ? 0 : 32 - __clz(run - 1);
+  return g;
+}
+template <typename T>
+MPM_DI T seg_scan(T v, const WarpSeg& g) {
+  const int lane = threadIdx.x & 31;
+  for (int i = 0, d = 1; i < g.steps; ++i, d <<= 1) {
+    const T t = __shfl_up_sync(0xffffffffu, v, d);
+    if (lane - d >= g.start) v += t;
+  }
+  return v;
+}
+template <typename T>
+MPM_DI void zero_stencil(Stencil<T>& s) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    s.base[d] = 0;
+    s.fx[d] = T(1);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) s.w[k][d] = T(0);
+  }
+}
+template <typename T>
+MPM_DI long long cell_key(const Consts<T>& c, int scene, const Stencil<T>& s) {
+  return (long long)scene * c.G + ((long long)s.base[0] * c.n_grid + s.base[1]) * c.n_grid + s.base[2];
 }
 
 template <typename T>
@@ -262,51 +351,67 @@ MPM_DI MatConsts<S> mat_consts(const Consts<T>& c) {
 template <typename T, typename S>
 __global__ void __launch_bounds__(128) k_p2g(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
                                              const int* __restrict__ pscene, Node<T>* __restrict__ grid) {
-  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= c.n_particles) return;
-  T x[3], v[3];
-  S C[9], F[9];
-  load_row(st, c.ld, p, 0, 3, x);
-  load_row(st, c.ld, p, 3, 3, v);
-#pragma unroll
-  for (int k = 0; k < 9; ++k) {
-    C[k] = S(st[(int64_t)(6 + k) * c.ld + p]);
-    F[k] = S(st[(int64_t)(15 + k) * c.ld + p]);
-  }
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = p < c.n_particles;  // every lane stays for the warp scan
   Stencil<T> s;
-  bool ok = make_stencil(c, x, s);
-  MatConsts<S> m = mat_consts<T, S>(c);
-  P2G<S> P;
-  S aff[9];
-  p2g_particle(m, C, F, P, aff);
-  if (st_out) {
+  zero_stencil(s);
+  bool ok = false;
+  int scene = 0;
+  T affine[9], pm[3] = {T(0), T(0), T(0)};
 #pragma unroll
-    for (int k = 0; k < 9; ++k) st_out[(int64_t)(15 + k) * c.ld + p] = T(P.newF[k]);
+  for (int k = 0; k < 9; ++k) affine[k] = T(0);
+  if (valid) {
+    T x[3], v[3];
+    S C[9], F[9];
+    load_row(st, c.ld, p, 0, 3, x);
+    load_row(st, c.ld, p, 3, 3, v);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      C[k] = S(st[(int64_t)(6 + k) * c.ld + p]);
+      F[k] = S(st[(int64_t)(15 + k) * c.ld + p]);
+    }
+    ok = make_stencil(c, x, s);
+    MatConsts<S> m = mat_consts<T, S>(c);
+    P2G<S> P;
+    S aff[9];
+    p2g_particle(m, C, F, P, aff);
+    if (st_out) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) st_out[(int64_t)(15 + k) * c.ld + p] = T(P.newF[k]);
+    }
+    if (!ok) atomicOr(c.status, MPM_STATUS_OUT_OF_GRID);
+    if (!finite(P.J)) atomicOr(c.status, MPM_STATUS_NONFINITE);
+    if (ok) {
+      scene = pscene[p];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) affine[k] = T(aff[k]);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) pm[k] = c.p_mass * v[k];
+    } else {
+      zero_stencil(s);
+    }
   }
-  if (!ok) {
-    atomicOr(c.status, MPM_STATUS_OUT_OF_GRID);
-    return;
-  }
-  if (!finite(P.J)) atomicOr(c.status, MPM_STATUS_NONFINITE);
-  T affine[9], pm[3];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) affine[k] = T(aff[k]);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) pm[k] = c.p_mass * v[k];
-  Node<T>* g = grid + (int64_t)pscene[p] * c.G;
+  const WarpSeg seg = warp_segments(ok ? cell_key(c, scene, s) : -1 - (long long)(threadIdx.x & 31));
+  Node<T>* g = grid + (int64_t)scene * c.G;
+  const StencilAddr A = stencil_addr(c, s);
 #pragma unroll
   for (int ox = 0; ox < 3; ++ox)
 #pragma unroll
     for (int oy = 0; oy < 3; ++oy)
 #pragma unroll
       for (int oz = 0; oz < 3; ++oz) {
-        T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
-        T dp[3] = {(T(ox) - s.fx[0]) * c.dx, (T(oy) - s.fx[1]) * c.dx, (T(oz) - s.fx[2]) * c.dx};
-        T mv[3];
+        const T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
+        const T dp[3] = {(T(ox) - s.fx[0]) * c.dx, (T(oy) - s.fx[1]) * c.dx, (T(oz) - s.fx[2]) * c.dx};
+        T mv[4];
 #pragma unroll
         for (int k = 0; k < 3; ++k)
           mv[k] = wgt * (pm[k] + affine[3 * k] * dp[0] + affine[3 * k + 1] * dp[1] + affine[3 * k + 2] * dp[2]);
-        atomic_add_node(g + node_of(c, s, ox, oy, oz), mv[0], mv[1], mv[2], wgt * c.p_mass);
+        mv[3] = wgt * c.p_mass;
+        if (seg.steps) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) mv[k] = seg_scan(mv[k], seg);
+        }
+        if (ok && seg.tail) atomic_add_node(g + A.at(ox, oy, oz), mv[0], mv[1], mv[2], mv[3]);
       }
 }
 
@@ -431,33 +536,50 @@ MPM_DI void walls_vjp(const Consts<T>& c, const int* I, const WallTape<T>& tp, T
   }
 }
 
+// Per-CTA tool table, reloaded when the block's scene changes.
 template <typename T>
-__global__ void __launch_bounds__(128) k_grid_op(Consts<T> c, const Node<T>* __restrict__ grid_in,
-                                                 Node<T>* __restrict__ grid_out,
-                                                 const MpmToolDesc* __restrict__ tools,
-                                                 const int* __restrict__ tool_off, const double* __restrict__ pose_f,
-                                                 const double* __restrict__ pose_f1) {
-  __shared__ SceneTools<T> sh;
-  int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // G % blockDim == 0
-  int scene = (int)(((int64_t)blockIdx.x * blockDim.x) / c.G);
-  load_scene_tools(sh, scene, tools, tool_off, pose_f, pose_f1);
-  Node<T> in = grid_in[gid];
-  Node<T> out = {T(0), T(0), T(0), in.w};
-  if (in.w > T(1e-12)) {
-    int64_t id = gid - (int64_t)scene * c.G;
-    int I[3] = {(int)(id / ((int64_t)c.n_grid * c.n_grid)), (int)((id / c.n_grid) % c.n_grid),
-                (int)(id % c.n_grid)};
-    T inv = T(1) / in.w;
-    T v[3] = {inv * in.x + c.gdt[0], inv * in.y + c.gdt[1], inv * in.z + c.gdt[2]};
-    const T p[3] = {T(I[0]) * c.dx, T(I[1]) * c.dx, T(I[2]) * c.dx};
-    for (int t = 0; t < sh.n; ++t) tool_collide(sh.tool[t], sh.p0[t], sh.p1[t], p, c.dt, v);
-    walls(c, I, v, (WallTape<T>*)nullptr);
-    if (!(finite(v[0]) && finite(v[1]) && finite(v[2]))) atomicOr(c.status, MPM_STATUS_NONFINITE);
-    out.x = v[0];
-    out.y = v[1];
-    out.z = v[2];
+MPM_DI void scene_tools_for(SceneTools<T>& sh, int& cur, int scene, const MpmToolDesc* __restrict__ tools,
+                            const int* __restrict__ tool_off, const double* __restrict__ pose_f,
+                            const double* __restrict__ pose_f1) {
+  __syncthreads();  // the previous block is done with sh
+  if (scene != cur) {  // uniform: one block per CTA iteration
+    load_scene_tools(sh, scene, tools, tool_off, pose_f, pose_f1);
+    cur = scene;
   }
-  grid_out[gid] = out;
+}
+
+// grid_op over the active blocks: one 64-thread CTA per block, grid-stride
+template <typename T>
+__global__ void __launch_bounds__(64) k_grid_op(Consts<T> c, const int* __restrict__ active,
+                                                const int* __restrict__ n_active,
+                                                const Node<T>* __restrict__ grid_in, Node<T>* __restrict__ grid_out,
+                                                const MpmToolDesc* __restrict__ tools,
+                                                const int* __restrict__ tool_off, const double* __restrict__ pose_f,
+                                                const double* __restrict__ pose_f1) {
+  __shared__ SceneTools<T> sh;
+  int cur = -1;
+  const int na = *n_active;
+  for (int b = blockIdx.x; b < na; b += gridDim.x) {
+    const int64_t gb = active[b];
+    int I[3];
+    const int scene = block_node(c, gb, threadIdx.x, I);
+    scene_tools_for(sh, cur, scene, tools, tool_off, pose_f, pose_f1);
+    const int64_t idx = gb * 64 + threadIdx.x;
+    Node<T> in = grid_in[idx];
+    Node<T> out = {T(0), T(0), T(0), in.w};
+    if (in.w > T(1e-12)) {
+      T inv = T(1) / in.w;
+      T v[3] = {inv * in.x + c.gdt[0], inv * in.y + c.gdt[1], inv * in.z + c.gdt[2]};
+      const T p[3] = {T(I[0]) * c.dx, T(I[1]) * c.dx, T(I[2]) * c.dx};
+      for (int t = 0; t < sh.n; ++t) tool_collide(sh.tool[t], sh.p0[t], sh.p1[t], p, c.dt, v);
+      walls(c, I, v, (WallTape<T>*)nullptr);
+      if (!(finite(v[0]) && finite(v[1]) && finite(v[2]))) atomicOr(c.status, MPM_STATUS_NONFINITE);
+      out.x = v[0];
+      out.y = v[1];
+      out.z = v[2];
+    }
+    grid_out[idx] = out;
+  }
 }
 
 template <typename T>
@@ -474,6 +596,7 @@ __global__ void __launch_bounds__(128) k_g2p(Consts<T> c, const T* __restrict__ 
     return;
   }
   const Node<T>* g = grid + (int64_t)pscene[p] * c.G;
+  const StencilAddr A = stencil_addr(c, s);
   T nv[3] = {T(0), T(0), T(0)}, nC[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) nC[k] = T(0);
@@ -485,7 +608,7 @@ __global__ void __launch_bounds__(128) k_g2p(Consts<T> c, const T* __restrict__ 
 #pragma unroll
       for (int oz = 0; oz < 3; ++oz) {
         T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
-        Node<T> gv = g[node_of(c, s, ox, oy, oz)];
+        Node<T> gv = g[A.at(ox, oy, oz)];
         const T gvv[3] = {gv.x, gv.y, gv.z};
         const T dp[3] = {T(ox) - s.fx[0], T(oy) - s.fx[1], T(oz) - s.fx[2]};
 #pragma unroll
@@ -515,45 +638,60 @@ template <typename T>
 __global__ void __launch_bounds__(128) k_g2p_adj(Consts<T> c, const T* __restrict__ st, const T* __restrict__ g1,
                                                  T* __restrict__ g0, const int* __restrict__ pscene,
                                                  const Node<T>* __restrict__ grid, Node<T>* __restrict__ g_grid) {
-  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= c.n_particles) return;
-  T x[3];
-  load_row(st, c.ld, p, 0, 3, x);
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = p < c.n_particles;  // every lane stays for the warp scan
   Stencil<T> s;
-  if (!make_stencil(c, x, s)) {
-    const T z[3] = {T(0), T(0), T(0)};
-    store_row(g0, c.ld, p, 0, 3, z);
-    return;
+  zero_stencil(s);
+  bool ok = false;
+  int scene = 0;
+  T x[3] = {T(0), T(0), T(0)};
+  if (valid) {
+    load_row(st, c.ld, p, 0, 3, x);
+    ok = make_stencil(c, x, s);
+    if (ok) {
+      scene = pscene[p];
+    } else {
+      zero_stencil(s);
+      const T z[3] = {T(0), T(0), T(0)};
+      store_row(g0, c.ld, p, 0, 3, z);
+    }
   }
-  const int64_t off = (int64_t)pscene[p] * c.G;
+  const int64_t off = (int64_t)scene * c.G;
   const Node<T>* g = grid + off;
   Node<T>* gg = g_grid + off;
+  const StencilAddr A = stencil_addr(c, s);
   T nv[3] = {T(0), T(0), T(0)};
+  T gnv[3] = {T(0), T(0), T(0)}, gC[9], gx[3] = {T(0), T(0), T(0)};
 #pragma unroll
-  for (int ox = 0; ox < 3; ++ox)
+  for (int k = 0; k < 9; ++k) gC[k] = T(0);
+  if (ok) {
 #pragma unroll
-    for (int oy = 0; oy < 3; ++oy)
+    for (int ox = 0; ox < 3; ++ox)
 #pragma unroll
-      for (int oz = 0; oz < 3; ++oz) {
-        T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
-        Node<T> n = g[node_of(c, s, ox, oy, oz)];
-        nv[0] += wgt * n.x;
-        nv[1] += wgt * n.y;
-        nv[2] += wgt * n.z;
-      }
-  T gx1[3], gnv[3], gC[9], gx[3];
-  load_row(g1, c.ld, p, 0, 3, gx1);
-  load_row(g1, c.ld, p, 3, 3, gnv);
-  load_row(g1, c.ld, p, 6, 9, gC);
+      for (int oy = 0; oy < 3; ++oy)
 #pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    T t = x[i] + c.dt * nv[i];
-    T mn = (t < c.x_hi) ? t : c.x_hi;
-    bool pass = (t < c.x_hi) && (c.x_lo < mn);
-    T gt = pass ? gx1[i] : T(0);
-    gx[i] = gt;
-    gnv[i] += c.dt * gt;
+        for (int oz = 0; oz < 3; ++oz) {
+          T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
+          Node<T> n = g[A.at(ox, oy, oz)];
+          nv[0] += wgt * n.x;
+          nv[1] += wgt * n.y;
+          nv[2] += wgt * n.z;
+        }
+    T gx1[3];
+    load_row(g1, c.ld, p, 0, 3, gx1);
+    load_row(g1, c.ld, p, 3, 3, gnv);
+    load_row(g1, c.ld, p, 6, 9, gC);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      T t = x[i] + c.dt * nv[i];
+      T mn = (t < c.x_hi) ? t : c.x_hi;
+      bool pass = (t < c.x_hi) && (c.x_lo < mn);
+      T gt = pass ? gx1[i] : T(0);
+      gx[i] = gt;
+      gnv[i] += c.dt * gt;
+    }
   }
+  const WarpSeg seg = warp_segments(ok ? cell_key(c, scene, s) : -1 - (long long)(threadIdx.x & 31));
   const T k4 = T(4) * c.inv_dx;
   T gw[3][3];
 #pragma unroll
@@ -567,118 +705,108 @@ __global__ void __launch_bounds__(128) k_g2p_adj(Consts<T> c, const T* __restric
     for (int oy = 0; oy < 3; ++oy)
 #pragma unroll
       for (int oz = 0; oz < 3; ++oz) {
-        T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
+        const T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
         const T dp[3] = {T(ox) - s.fx[0], T(oy) - s.fx[1], T(oz) - s.fx[2]};
-        Node<T> n = g[node_of(c, s, ox, oy, oz)];
-        const T gv[3] = {n.x, n.y, n.z};
         T gCd[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) gCd[i] = gC[3 * i] * dp[0] + gC[3 * i + 1] * dp[1] + gC[3 * i + 2] * dp[2];
-        atomic_add_node3(gg + node_of(c, s, ox, oy, oz), wgt * (gnv[0] + k4 * gCd[0]), wgt * (gnv[1] + k4 * gCd[1]),
-                         wgt * (gnv[2] + k4 * gCd[2]));
-        T g_wgt = dot3(gv, gnv) + k4 * dot3(gv, gCd);
+        T sc3[3] = {wgt * (gnv[0] + k4 * gCd[0]), wgt * (gnv[1] + k4 * gCd[1]), wgt * (gnv[2] + k4 * gCd[2])};
+        if (seg.steps) {
 #pragma unroll
-        for (int j = 0; j < 3; ++j) gfx[j] -= k4 * wgt * (gC[j] * gv[0] + gC[3 + j] * gv[1] + gC[6 + j] * gv[2]);
-        gw[ox][0] += g_wgt * s.w[oy][1] * s.w[oz][2];
-        gw[oy][1] += g_wgt * s.w[ox][0] * s.w[oz][2];
-        gw[oz][2] += g_wgt * s.w[ox][0] * s.w[oy][1];
+          for (int k = 0; k < 3; ++k) sc3[k] = seg_scan(sc3[k], seg);
+        }
+        if (ok) {
+          if (seg.tail) atomic_add_node3(gg + A.at(ox, oy, oz), sc3[0], sc3[1], sc3[2]);
+          Node<T> n = g[A.at(ox, oy, oz)];
+          const T gv[3] = {n.x, n.y, n.z};
+          T g_wgt = dot3(gv, gnv) + k4 * dot3(gv, gCd);
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+            gfx[j] -= k4 * wgt * (gC[j] * gv[0] + gC[3 + j] * gv[1] + gC[6 + j] * gv[2]);
+          gw[ox][0] += g_wgt * s.w[oy][1] * s.w[oz][2];
+          gw[oy][1] += g_wgt * s.w[ox][0] * s.w[oz][2];
+          gw[oz][2] += g_wgt * s.w[ox][0] * s.w[oy][1];
+        }
       }
+  if (ok) {
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
+    for (int d = 0; d < 3; ++d) {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) gfx[d] += gw[k][d] * dweight(s, k, d);
-    gx[d] += c.inv_dx * gfx[d];
+      for (int k = 0; k < 3; ++k) gfx[d] += gw[k][d] * dweight(s, k, d);
+      gx[d] += c.inv_dx * gfx[d];
+    }
+    store_row(g0, c.ld, p, 0, 3, gx);
   }
-  store_row(g0, c.ld, p, 0, 3, gx);
 }
 
-// FP64 warp reduction of one value; lane 0 adds into shared accumulator
-MPM_DI void warp_add_to(double* acc, double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(acc, v);
-}
-
-// grid_op.grad: g_grid (velocity adjoint, xyz) -> g_in (mv.xyz, m); tool
-// pose gradients of frames f and f+1 reduced in FP64.
+// grid_op.grad over the active blocks: g_grid (velocity adjoint) -> g_in
+// (mv.xyz, m); tool-pose gradients of frames f and f+1 reduced per warp in
+// FP64 and added with one atomic per warp and component.
 template <typename T>
-__global__ void __launch_bounds__(128) k_grid_op_adj(Consts<T> c, const Node<T>* __restrict__ grid_in,
-                                                     const Node<T>* __restrict__ g_grid,
-                                                     Node<T>* __restrict__ g_in,
-                                                     const MpmToolDesc* __restrict__ tools,
-                                                     const int* __restrict__ tool_off,
-                                                     const double* __restrict__ pose_f,
-                                                     const double* __restrict__ pose_f1, double* __restrict__ g_pose_f,
-                                                     double* __restrict__ g_pose_f1) {
+__global__ void __launch_bounds__(64) k_grid_op_adj(Consts<T> c, const int* __restrict__ active,
+                                                    const int* __restrict__ n_active,
+                                                    const Node<T>* __restrict__ grid_in,
+                                                    const Node<T>* __restrict__ g_grid, Node<T>* __restrict__ g_in,
+                                                    const MpmToolDesc* __restrict__ tools,
+                                                    const int* __restrict__ tool_off,
+                                                    const double* __restrict__ pose_f,
+                                                    const double* __restrict__ pose_f1,
+                                                    double* __restrict__ g_pose_f, double* __restrict__ g_pose_f1) {
   __shared__ SceneTools<T> sh;
-  __shared__ double acc[MAX_TOOLS_PER_SCENE][16];
-  int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int scene = (int)(((int64_t)blockIdx.x * blockDim.x) / c.G);
-  for (int i = threadIdx.x; i < MAX_TOOLS_PER_SCENE * 16; i += blockDim.x) (&acc[0][0])[i] = 0.0;
-  load_scene_tools(sh, scene, tools, tool_off, pose_f, pose_f1);
-  Node<T> in = grid_in[gid];
-  Node<T> go = g_grid[gid];
-  bool active = in.w > T(1e-12) && (go.x != T(0) || go.y != T(0) || go.z != T(0));
-  Node<T> res = {T(0), T(0), T(0), T(0)};
-  int64_t id = gid - (int64_t)scene * c.G;
-  int I[3] = {(int)(id / ((int64_t)c.n_grid * c.n_grid)), (int)((id / c.n_grid) % c.n_grid), (int)(id % c.n_grid)};
-  const T p[3] = {T(I[0]) * c.dx, T(I[1]) * c.dx, T(I[2]) * c.dx};
-  T vt[MAX_TOOLS_PER_SCENE + 1][3];
-  WallTape<T> wt;
-  T g[3] = {go.x, go.y, go.z};
-  T inv = T(1) / in.w;
-  if (active) {
-    T v[3] = {inv * in.x + c.gdt[0], inv * in.y + c.gdt[1], inv * in.z + c.gdt[2]};
-    for (int t = 0; t < sh.n; ++t) {
+  int cur = -1;
+  const int na = *n_active;
+  for (int b = blockIdx.x; b < na; b += gridDim.x) {
+    const int64_t gb = active[b];
+    int I[3];
+    const int scene = block_node(c, gb, threadIdx.x, I);
+    scene_tools_for(sh, cur, scene, tools, tool_off, pose_f, pose_f1);
+    const int64_t idx = gb * 64 + threadIdx.x;
+    Node<T> in = grid_in[idx];
+    Node<T> go = g_grid[idx];
+    const bool active_node = in.w > T(1e-12) && (go.x != T(0) || go.y != T(0) || go.z != T(0));
+    const T p[3] = {T(I[0]) * c.dx, T(I[1]) * c.dx, T(I[2]) * c.dx};
+    T vt[MAX_TOOLS_PER_SCENE + 1][3];
+    WallTape<T> wt;
+    T g[3] = {go.x, go.y, go.z};
+    const T inv = active_node ? T(1) / in.w : T(0);
+    if (active_node) {
+      T v[3] = {inv * in.x + c.gdt[0], inv * in.y + c.gdt[1], inv * in.z + c.gdt[2]};
+      for (int t = 0; t < sh.n; ++t) {
 #pragma unroll
-      for (int k = 0; k < 3; ++k) vt[t][k] = v[k];
-      tool_collide(sh.tool[t], sh.p0[t], sh.p1[t], p, c.dt, v);
+        for (int k = 0; k < 3; ++k) vt[t][k] = v[k];
+        tool_collide(sh.tool[t], sh.p0[t], sh.p1[t], p, c.dt, v);
+      }
+      walls(c, I, v, &wt);
+      walls_vjp(c, I, wt, g);
     }
-    walls(c, I, v, &wt);
-    walls_vjp(c, I, wt, g);
-  }
-  const int nt = sh.n;
-  for (int t = nt - 1; t >= 0; --t) {
-    PoseGrad<T> g0, g1;
-    g0.zero();
-    g1.zero();
-    if (active) tool_collide_vjp(sh.tool[t], sh.p0[t], sh.p1[t], p, c.dt, vt[t], g, g0, g1);
-    const bool any = __any_sync(0xffffffffu, active);
-    if (any) {
-      warp_add_to(&acc[t][0], double(g0.pos[0]));
-      warp_add_to(&acc[t][1], double(g0.pos[1]));
-      warp_add_to(&acc[t][2], double(g0.pos[2]));
-      warp_add_to(&acc[t][3], double(g0.rot[0]));
-      warp_add_to(&acc[t][4], double(g0.rot[1]));
-      warp_add_to(&acc[t][5], double(g0.rot[2]));
-      warp_add_to(&acc[t][6], double(g0.rot[3]));
-      warp_add_to(&acc[t][7], double(g0.gap));
-      warp_add_to(&acc[t][8], double(g1.pos[0]));
-      warp_add_to(&acc[t][9], double(g1.pos[1]));
-      warp_add_to(&acc[t][10], double(g1.pos[2]));
-      warp_add_to(&acc[t][11], double(g1.rot[0]));
-      warp_add_to(&acc[t][12], double(g1.rot[1]));
-      warp_add_to(&acc[t][13], double(g1.rot[2]));
-      warp_add_to(&acc[t][14], double(g1.rot[3]));
-      warp_add_to(&acc[t][15], double(g1.gap));
+    const int t0 = tool_off[scene];
+    for (int t = sh.n - 1; t >= 0; --t) {
+      PoseGrad<T> g0, g1;
+      g0.zero();
+      g1.zero();
+      if (active_node) tool_collide_vjp(sh.tool[t], sh.p0[t], sh.p1[t], p, c.dt, vt[t], g, g0, g1);
+      if (__any_sync(0xffffffffu, active_node)) {
+        double* d0 = g_pose_f + 8 * (t0 + t);
+        double* d1 = g_pose_f1 + 8 * (t0 + t);
+        const T v16[16] = {g0.pos[0], g0.pos[1], g0.pos[2], g0.rot[0], g0.rot[1], g0.rot[2], g0.rot[3], g0.gap,
+                           g1.pos[0], g1.pos[1], g1.pos[2], g1.rot[0], g1.rot[1], g1.rot[2], g1.rot[3], g1.gap};
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          double v = double(v16[k]);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+          if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd((k < 8 ? d0 + k : d1 + (k - 8)), v);
+        }
+      }
     }
-  }
-  if (active) {
-    res.x = g[0] * inv;
-    res.y = g[1] * inv;
-    res.z = g[2] * inv;
-    res.w = -(g[0] * in.x + g[1] * in.y + g[2] * in.z) * inv * inv;
-  }
-  g_in[gid] = res;
-  __syncthreads();
-  int t0 = tool_off[scene];
-  for (int i = threadIdx.x; i < nt * 16; i += blockDim.x) {
-    int t = i / 16, k = i % 16;
-    double v = acc[t][k];
-    if (v != 0.0) {
-      double* dst = (k < 8) ? (g_pose_f + 8 * (t0 + t) + k) : (g_pose_f1 + 8 * (t0 + t) + (k - 8));
-      atomicAdd(dst, v);
+    Node<T> res = {T(0), T(0), T(0), T(0)};
+    if (active_node) {
+      res.x = g[0] * inv;
+      res.y = g[1] * inv;
+      res.z = g[2] * inv;
+      res.w = -(g[0] * in.x + g[1] * in.y + g[2] * in.z) * inv * inv;
     }
+    g_in[idx] = res;
   }
 }
 
@@ -715,6 +843,7 @@ __global__ void __launch_bounds__(128) k_p2g_adj(Consts<T> c, const T* __restric
   for (int k = 0; k < 9; ++k) g_aff[k] = S(0);
   if (ok) {
     const Node<T>* gg = g_in + (int64_t)pscene[p] * c.G;
+    const StencilAddr A = stencil_addr(c, s);
     T ga[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) ga[k] = T(0);
@@ -732,7 +861,7 @@ __global__ void __launch_bounds__(128) k_p2g_adj(Consts<T> c, const T* __restric
         for (int oz = 0; oz < 3; ++oz) {
           T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
           const T dp[3] = {(T(ox) - s.fx[0]) * c.dx, (T(oy) - s.fx[1]) * c.dx, (T(oz) - s.fx[2]) * c.dx};
-          Node<T> n = gg[node_of(c, s, ox, oy, oz)];
+          Node<T> n = gg[A.at(ox, oy, oz)];
           const T gn[3] = {n.x, n.y, n.z};
           T contrib[3];
 #pragma unroll
@@ -771,6 +900,59 @@ __global__ void __launch_bounds__(128) k_p2g_adj(Consts<T> c, const T* __restric
   for (int k = 0; k < 9; ++k) {
     g0[(int64_t)(6 + k) * c.ld + p] = T(gC[k]);
     g0[(int64_t)(15 + k) * c.ld + p] = T(gF[k]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// active-block bookkeeping
+// ---------------------------------------------------------------------------
+// flags[scene*NB3 + block] = 1 for every block a particle stencil touches
+template <typename T>
+__global__ void __launch_bounds__(256) k_mark_blocks(Consts<T> c, const T* __restrict__ st,
+                                                     const int* __restrict__ pscene,
+                                                     unsigned char* __restrict__ flags) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= c.n_particles) return;
+  T x[3];
+  load_row(st, c.ld, p, 0, 3, x);
+  Stencil<T> s;
+  if (!make_stencil(c, x, s)) return;  // skipped (and flagged) by the scatter
+  int lo[3], hi[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = s.base[d] >> 2;
+    hi[d] = (s.base[d] + 2) >> 2;
+  }
+  unsigned char* f = flags + (int64_t)pscene[p] * c.NB3;
+  const int nb = c.nb;
+  for (int bi = lo[0]; bi <= hi[0]; ++bi)
+    for (int bj = lo[1]; bj <= hi[1]; ++bj)
+      for (int bk = lo[2]; bk <= hi[2]; ++bk) f[((int64_t)bi * nb + bj) * nb + bk] = 1;
+}
+// list of flagged blocks (warp-aggregated append; order is not significant)
+static __global__ void __launch_bounds__(256) k_compact_blocks(const unsigned char* __restrict__ flags, int64_t total,
+                                                        int* __restrict__ active, int* __restrict__ counter) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool f = i < total && flags[i] != 0;
+  const unsigned m = __ballot_sync(0xffffffffu, f);
+  if (m == 0) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(counter, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (f) active[base + __popc(m & ((1u << lane) - 1u))] = (int)i;
+}
+// zero the listed blocks of one or two grids
+template <typename T>
+__global__ void __launch_bounds__(256) k_clear_blocks(const int* __restrict__ active, const int* __restrict__ n_active,
+                                                      Node<T>* __restrict__ a, Node<T>* __restrict__ b) {
+  const int64_t n = (int64_t)(*n_active) * 64;
+  const Node<T> z = {T(0), T(0), T(0), T(0)};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t idx = (int64_t)active[i >> 6] * 64 + (i & 63);
+    a[idx] = z;
+    if (b) b[idx] = z;
   }
 }
 

@@ -37,9 +37,12 @@ struct LaunchCtx {
   const int* tool_off;         // [n_scenes + 1] device
   unsigned int* status;        // sticky status word
   void* grid_a;                // scratch grids, n_scenes*G nodes of 4 reals
-  void* grid_b;
+  void* grid_b;                //   (block-contiguous layout, see mpm_kernels.cuh)
   void* grid_c;
   void* grid_d;
+  unsigned char* blockbuf;     // [16-byte counter header][n_scenes * NB3 block flags]
+  int* active;                 // [n_scenes * NB3] list of active blocks
+  int sm_count;                // multiprocessors of the device (grid-stride launch sizes)
   cudaStream_t stream;
   int64_t* launches;           // launch counter
   Profiler* prof;              // may be null
@@ -60,6 +63,12 @@ struct LaunchCtx {
     prof_end((L).prof, _slot, MPM_K_CLEAR, (L).stream);                \
     if (_e != cudaSuccess) return _e;                                  \
   } while (0)
+
+// bytes of the block-flag buffer (counter header + one flag per block)
+inline size_t blockbuf_bytes(int64_t n_scenes, int n_grid) {
+  const int64_t nb = n_grid / 4;
+  return 16 + (size_t)(n_scenes * nb * nb * nb);
+}
 
 template <typename T, typename S>
 cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const double* pose_f,

@@ -11,11 +11,12 @@
 // so those callers use this entry point instead; they still pass the state,
 // tool poses and output buffers, which they own.
 //
-// The scratch is the file-scope array g_static_scratch below.  Every GPU that
+// The scratch is the file-scope array g_static_scratch below (20 MiB + 64 KiB).  Every GPU that
 // loads this library holds it until the process exits.  All calls share it
-// and it keeps the last call's contents: the status word and the grid that
-// accumulates the scatter are cleared on every call, the scene-index region
-// is zeroed once per device and never written afterwards.  Calls whose
+// and it keeps the last call's contents: the status word, the active-block
+// flags and the grid blocks the scatter accumulates into are cleared on every
+// call; the scene-index region is zeroed once per device and never written
+// afterwards.  Calls whose
 // kernels overlap on the GPU (different streams, or different host threads,
 // on the same device) race on the array; serialise them.
 #include <cuda_runtime.h>
@@ -34,13 +35,20 @@ namespace {
 //   [0, 4)                      status word
 //   [16, 24)                    tool offsets {0, n_tools} of the one scene
 //   [256, 256 + 8*tool size)    tool table
+//   [4096, 4096 + 16 + 8000)    active-block counter and flags (<= 20^3 blocks)
+//   [16384, 16384 + 32000)      active-block list
 //   [kHeader, +kScene)          zero scene index of every particle
 //   [kHeader+kScene, +kGrids)   forward grid (mv, m) then velocity grid
-constexpr size_t kHeader = 8192;
+constexpr size_t kBlockBuf = 4096;
+constexpr size_t kActive = 16384;
+constexpr int64_t kMaxBlocks = 8000;  // (80/4)^3
+constexpr size_t kHeader = 65536;
 constexpr int64_t kMaxParticles = int64_t(1) << 20;             // 1,048,576 particles
 constexpr size_t kScene = size_t(kMaxParticles) * sizeof(int);  // 4 MiB
 constexpr size_t kGrids = size_t(16) << 20;                     // 16 MiB for the two grids
-constexpr size_t kScratchBytes = kHeader + kScene + kGrids;     // 20 MiB + 8 KiB
+constexpr size_t kScratchBytes = kHeader + kScene + kGrids;     // 20 MiB + 64 KiB
+static_assert(kBlockBuf + 16 + kMaxBlocks <= kActive, "block flags overlap the list");
+static_assert(kActive + kMaxBlocks * sizeof(int) <= kHeader, "block list overlaps the scene index");
 
 static __device__ __align__(256) unsigned char g_static_scratch[kScratchBytes];
 
@@ -101,6 +109,8 @@ int mpm_substep_fwd_static(const MpmParams* params, const MpmToolDesc* tools, in
     return set_err(MPM_E_INVALID, "mpm_substep_fwd_static: two grids of n_grid^3 nodes need " +
                                       std::to_string(2 * grid_bytes) + " bytes, above the static limit of " +
                                       std::to_string(kGrids) + " (n_grid <= 80 in FP32, <= 64 in FP64)");
+  if ((int64_t)(p.n_grid / 4) * (p.n_grid / 4) * (p.n_grid / 4) > kMaxBlocks)
+    return set_err(MPM_E_INVALID, "mpm_substep_fwd_static: n_grid above the static limit of 80");
   if (p.n_particles < 0 || p.n_particles > kMaxParticles)
     return set_err(MPM_E_INVALID, "mpm_substep_fwd_static: n_particles must be in [0, " +
                                       std::to_string(kMaxParticles) + "]");
@@ -141,10 +151,15 @@ int mpm_substep_fwd_static(const MpmParams* params, const MpmToolDesc* tools, in
   L.tools = reinterpret_cast<const MpmToolDesc*>(base + 256);
   L.tool_off = reinterpret_cast<const int*>(base + 16);
   L.status = reinterpret_cast<unsigned int*>(base);
-  L.grid_a = base + kHeader + kScene;              // cleared by the launcher before the scatter
+  L.grid_a = base + kHeader + kScene;              // active blocks cleared by the launcher before the scatter
   L.grid_b = base + kHeader + kScene + grid_bytes;  // fully written by grid_op
   L.grid_c = nullptr;
   L.grid_d = nullptr;
+  L.blockbuf = base + kBlockBuf;  // cleared by the launcher every call
+  L.active = reinterpret_cast<int*>(base + kActive);
+  int sm = 1;
+  if (cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sm < 1) sm = 1;
+  L.sm_count = sm;
   L.stream = s;
   L.launches = &launches;
   L.prof = nullptr;

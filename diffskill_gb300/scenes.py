@@ -10,7 +10,8 @@ Workloads (sizes from the project's benchmark definitions):
 
 * ``config1``: FP64 single scene, 64^3, dt=5e-4, 10k particles, one capsule.
 * ``config2``: single scene, 64^3, 30k particles, box spatula + capsule pin.
-* ``config3``: 64 batched scenes, 5k-40k particles each, 1-3 tools each.
+* ``config3``: 64 batched scenes, 5k-40k particles each, 1-3 tools each
+  (every tool starts resting on a dough blob).
 * ``config4``: 128^3 cutting/gripping scene, 100k particles, knife + gripper.
 * ``config5``: 16 batched 128^3 scenes, 100k-500k particles, 3 tools each.
 """
@@ -138,25 +139,33 @@ def config2(n_actions: int = 50, n_particles: int = 30000, substeps: int = 50, d
                           substeps=substeps, precision=precision, n_particles=n_particles)
     rng = np.random.default_rng(seed)
     x0 = sample_box(rng, n_particles, (0.5, 0.09, 0.5), (0.25, 0.08, 0.25))
-    tools = [box((0.5, 0.16, 0.5), (0.075, 0.0025, 0.075)),
-             capsule((0.3, 0.165, 0.5), r=0.03, h=0.25)]
+    # both tools rest on the slab top (y = 0.13), pressing 3 mm into it
+    tools = [box((0.5, 0.1295, 0.5), (0.075, 0.0025, 0.075)),
+             capsule((0.3, 0.157, 0.5), r=0.03, h=0.25)]
     actions = rng.uniform(-1, 1, size=(n_actions, 6))
     tx = sample_box(rng, n_particles, (0.5, 0.07, 0.5), (0.35, 0.04, 0.35))
     target = density_grid(clip_particles(tx, sim), sim.grid, sim.p_mass)
     return Scene(sim, tools, clip_particles(x0, sim), target, actions, checkpoint_every=10, name="config2")
 
 
-def _random_tools(rng: np.random.Generator, k: int, top: float) -> List[PrimitiveConfig]:
+def _random_tools(rng: np.random.Generator, k: int, blobs) -> List[PrimitiveConfig]:
+    """``k`` tools of random type and size, each resting on top of one dough
+    blob (``blobs``: list of (centre, half-height)) and pressing 5 mm into it,
+    so every tool is in contact from the first substep."""
     tools = []
     for _ in range(k):
+        (cx, cy, cz), hh = blobs[int(rng.integers(0, len(blobs)))]
+        top = cy + hh
+        dx, dz = rng.uniform(-0.5, 0.5, size=2) * hh
         kind = rng.integers(0, 3)
-        pos = (float(rng.uniform(0.3, 0.7)), float(top + rng.uniform(0.03, 0.08)), float(rng.uniform(0.3, 0.7)))
         if kind == 0:
-            tools.append(sphere(pos, radius=float(rng.uniform(0.03, 0.06))))
+            r = float(rng.uniform(0.03, 0.06))
+            tools.append(sphere((cx + dx, top + r - 0.005, cz + dz), radius=r))
         elif kind == 1:
-            tools.append(capsule(pos, r=0.03, h=float(rng.uniform(0.2, 0.25))))
+            tools.append(capsule((cx + dx, top + 0.03 - 0.005, cz + dz), r=0.03, h=float(rng.uniform(0.2, 0.25))))
         else:
-            tools.append(box(pos, (float(rng.uniform(0.02, 0.075)), 0.0025, float(rng.uniform(0.02, 0.075)))))
+            tools.append(box((cx + dx, top + 0.0025 - 0.005, cz + dz),
+                             (float(rng.uniform(0.02, 0.075)), 0.0025, float(rng.uniform(0.02, 0.075)))))
     return tools
 
 
@@ -174,13 +183,13 @@ def config3(n_scenes: int = 64, n_actions: int = 20, substeps: int = 50, dt: Opt
         vol = radii ** 3
         counts = np.floor(n * vol / vol.sum()).astype(int)
         counts[0] += n - counts.sum()
-        parts = []
+        parts, blobs = [], []
         for r, c in zip(radii, counts):
             centre = (rng.uniform(0.3, 0.6), 0.05 + r, rng.uniform(0.3, 0.7))
             parts.append(sample_sphere(rng, int(c), centre, float(r)))
+            blobs.append((centre, float(r)))
         x0 = clip_particles(np.concatenate(parts), sim)
-        top = float(x0[:, 1].max())
-        tools = _random_tools(rng, int(rng.integers(1, 4)), top)
+        tools = _random_tools(rng, int(rng.integers(1, 4)), blobs)
         adim = action_dims(tools)[-1]
         actions = rng.uniform(-1, 1, size=(n_actions, adim))
         target = density_grid(clip_particles(x0 + np.array([0.1, 0.0, 0.0]), sim), sim.grid, sim.p_mass)
@@ -222,12 +231,16 @@ def config5(n_scenes: int = 16, n_actions: int = 100, substeps: int = 50, dt: Op
         if rng.random() < 0.5:
             w = rng.uniform(0.15, 0.3, size=3)
             w[1] = rng.uniform(0.06, 0.12)
-            x0 = sample_box(rng, n, (rng.uniform(0.35, 0.65), 0.04 + w[1] / 2, rng.uniform(0.35, 0.65)), w)
+            centre = (rng.uniform(0.35, 0.65), 0.04 + w[1] / 2, rng.uniform(0.35, 0.65))
+            x0 = sample_box(rng, n, centre, w)
+            blob = (centre, float(w[1] / 2))
         else:
             r = rng.uniform(0.08, 0.14)
-            x0 = sample_sphere(rng, n, (rng.uniform(0.35, 0.65), 0.04 + r, rng.uniform(0.35, 0.65)), r)
+            centre = (rng.uniform(0.35, 0.65), 0.04 + r, rng.uniform(0.35, 0.65))
+            x0 = sample_sphere(rng, n, centre, r)
+            blob = (centre, float(r))
         x0 = clip_particles(x0, sim)
-        tools = _random_tools(rng, 3, float(x0[:, 1].max()))
+        tools = _random_tools(rng, 3, [blob])
         adim = action_dims(tools)[-1]
         actions = rng.uniform(-1, 1, size=(n_actions, adim))
         target = density_grid(clip_particles(x0 + np.array([0.1, 0.0, 0.0]), sim), sim.grid, sim.p_mass)

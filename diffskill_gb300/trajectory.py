@@ -12,10 +12,22 @@ from __future__ import annotations
 
 from typing import List, Optional, Sequence
 
+import numpy as np
 import torch
 
 from .engine import Horizon, MpmEngine
 from .scenes import Scene
+
+
+def spatial_order(x: np.ndarray, n_grid: int) -> np.ndarray:
+    """Permutation sorting particles by base cell, block-major (4^3 cells per
+    block, then cell within block), so that neighbouring threads of the p2g
+    scatter and the g2p gather touch the same grid nodes."""
+    base = np.clip((np.asarray(x) * n_grid - 0.5).astype(np.int64), 0, n_grid - 1)
+    nb = n_grid // 4
+    blk = ((base[:, 0] >> 2) * nb + (base[:, 1] >> 2)) * nb + (base[:, 2] >> 2)
+    loc = ((base[:, 0] & 3) << 4) | ((base[:, 1] & 3) << 2) | (base[:, 2] & 3)
+    return np.argsort(blk * 64 + loc, kind="stable")
 
 
 def _check_compatible(scenes: Sequence[Scene]) -> None:
@@ -32,7 +44,7 @@ def _check_compatible(scenes: Sequence[Scene]) -> None:
 
 class BatchedTrajectory:
     def __init__(self, scenes: Sequence[Scene], ckpt_every: Optional[int] = None, lr: float = 0.01,
-                 betas=(0.9, 0.999), eps: float = 1e-8, softness: float = 666.0):
+                 betas=(0.9, 0.999), eps: float = 1e-8, softness: float = 666.0, sort_particles: bool = True):
         scenes = list(scenes)
         _check_compatible(scenes)
         self.scenes = scenes
@@ -41,7 +53,10 @@ class BatchedTrajectory:
         k = ckpt_every if ckpt_every else (scenes[0].checkpoint_every or scenes[0].sim.n_substeps)
         self.hz = Horizon(self.eng, scenes[0].n_actions, ckpt_every=k)
         eng = self.eng
-        self.state0 = eng.init_state([sc.x0 for sc in scenes])
+        # particle order is internal: losses and action gradients do not depend on it
+        self.orders = [spatial_order(sc.x0, eng.n_grid) if sort_particles else np.arange(sc.n_particles)
+                       for sc in scenes]
+        self.state0 = eng.init_state([sc.x0[o] for sc, o in zip(scenes, self.orders)])
         self.targets = eng.targets([sc.target for sc in scenes])
         self.actions = eng.expand_actions([sc.actions for sc in scenes])
         mask = torch.zeros((1, max(eng.T, 1), 8), dtype=torch.float64, device=eng.device)

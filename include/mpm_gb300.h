@@ -180,7 +180,7 @@ int mpm_tool_distance_bwd(MpmHandle* h, const void* state, const double* pose, c
  * of cudaMalloc/cudaFree.  No handle: params (n_scenes = 1) and the host tool
  * table are passed per call; the caller still owns state_f, state_f1, pose_f
  * and pose_f1.  Grid scratch, tool table and status word live in one
- * file-scope static device array of 20 MiB + 8 KiB, held by every GPU that
+ * file-scope static device array of 20 MiB + 64 KiB, held by every GPU that
  * loads the library until the process exits.  Limits: n_particles <= 2^20;
  * two grids of n_grid^3 nodes within 16 MiB (n_grid <= 80 in FP32, <= 64 in
  * FP64); at most 8 tools.  Larger sizes return MPM_E_INVALID; the message is
