@@ -42,7 +42,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["config3", "config2", "config1"], default="config3")
+    ap.add_argument("--workload", choices=["config3", "config3-small", "config2", "config1"], default="config3")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip plain-FP64 / accuracy / CPU legs")
     ap.add_argument("--ckpt", type=int, default=0, help="checkpoint interval (0 = choose by memory budget)")
@@ -60,6 +60,12 @@ def make_workload(name: str, rank: int, precision: str = "fp32"):
                             "1-4 dough spheres + 1-3 tools per scene, 64^3 grid, 20 actions x 50 substeps, "
                             "dt=1e-4, FP32, fwd+loss+adjoint+Adam per step",
                 "scenes": len(scs)}
+    elif name == "config3-small":  # profiling case: a few GB on the device
+        scs = scenes.config3(seed=1003 + 7919 * rank, precision=precision)[:16]
+        for sc in scs:
+            sc.actions = sc.actions[:2]
+        desc = {"workload": "config3-small: the first 16 scenes of config3, 2 actions x 50 substeps, FP32 "
+                            "(profiling case)", "scenes": len(scs)}
     elif name == "config2":
         scs = [scenes.config2(seed=1002 + 7919 * rank, precision=precision)]
         desc = {"workload": "config2: single scene, 30k particles, box spatula + capsule, 64^3, "
@@ -197,7 +203,7 @@ def run_ours(args, rank, world, dist):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     scs, desc = make_workload(args.workload, rank)
-    k = args.ckpt or choose_checkpoint(scs)
+    k = args.ckpt or (10 if args.workload == "config3-small" else choose_checkpoint(scs))
     bt = BatchedTrajectory(scs, ckpt_every=k)
     eng = bt.eng
     ps = bt.particle_substeps  # per iteration on this rank

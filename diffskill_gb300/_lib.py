@@ -43,6 +43,11 @@ class MpmToolDesc(ctypes.Structure):
                 ("action_scale", _f64 * 7)]
 
 
+class MpmGridStore(ctypes.Structure):
+    _fields_ = [("blocks", _c_p), ("block_ids", _c_p), ("slot_start", _c_p), ("slot_count", _c_p), ("bump", _c_p),
+                ("capacity", _i64), ("n_slots", _i32), ("reserved", _i32)]
+
+
 # every exported entry point and its ctypes signature
 SIGNATURES = {
     "mpm_version": (ctypes.c_char_p, []),
@@ -53,6 +58,9 @@ SIGNATURES = {
     "mpm_tools_action_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _i32, _c_p]),
     "mpm_substep_fwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_substep_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
+    "mpm_substep_fwd_store": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, ctypes.POINTER(MpmGridStore), _i32, _c_p]),
+    "mpm_substep_bwd_store": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, ctypes.POINTER(MpmGridStore),
+                                     _i32, _c_p]),
     "mpm_grid_mass": (_i32, [_c_p, _c_p, _c_p, _c_p]),
     "mpm_grid_mass_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_density_l1": (_i32, [_c_p, _c_p, _c_p, _f64, _c_p, _c_p, _c_p]),

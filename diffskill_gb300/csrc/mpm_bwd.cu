@@ -8,14 +8,16 @@ namespace mpm {
 template <typename T>
 Consts<T> make_consts(const LaunchCtx& L);  // mpm_fwd.cu
 template <typename T>
-cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* b);
+cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* b,
+                           const MpmGridStore* store, int slot);
 unsigned grid_blocks_launch(const LaunchCtx& L, int64_t total_blocks);
 
 static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 template <typename T, typename S>
 cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* g1, T* g0, const double* pose_f,
-                               const double* pose_f1, double* g_pose_f, double* g_pose_f1) {
+                               const double* pose_f1, double* g_pose_f, double* g_pose_f1, const MpmGridStore* store,
+                               int slot) {
   Consts<T> c = make_consts<T>(L);
   Node<T>* gin = (Node<T>*)L.grid_a;
   Node<T>* gout = (Node<T>*)L.grid_b;
@@ -25,10 +27,11 @@ cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* g1, T*
   const unsigned pb = blocks_for(c.n_particles, 128);
   const unsigned gb = grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3);
   // recompute the grid of this substep (substep_grad, mpm_simulator.py:327-333)
-  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, g_gout);
+  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, g_gout, store, slot);
   if (e != cudaSuccess) return e;
   if (c.n_particles > 0)
-    MPM_LAUNCH(L, MPM_K_P2G_RECOMP, (k_p2g<T, S>), pb, 128, c, st0, (T*)nullptr, L.pscene, gin);
+    MPM_LAUNCH(L, MPM_K_P2G_RECOMP, (k_p2g<T, S>), pb, 128, c, st0, (T*)nullptr, L.pscene, gin,
+               store ? store->slot_start + slot : (const int64_t*)nullptr);
   MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, gb, 64, c, L.active, counter, gin, gout, L.tools, L.tool_off, pose_f,
              pose_f1);
   if (c.n_particles > 0)
@@ -162,7 +165,7 @@ template cudaError_t launch_tool_distance_bwd<double>(const LaunchCtx&, const in
 
 #define MPM_INST_BWD(T, S)                                                                                  \
   template cudaError_t launch_substep_bwd<T, S>(const LaunchCtx&, const T*, const T*, T*, const double*, \
-                                                const double*, double*, double*);
+                                                const double*, double*, double*, const MpmGridStore*, int);
 MPM_INST_BWD(float, float)
 MPM_INST_BWD(float, double)
 MPM_INST_BWD(double, double)

@@ -378,8 +378,17 @@ int mpm_tools_action_bwd(MpmHandle* h, const double* vel, const double* pose, do
   return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_tools_action_bwd");
 }
 
-int mpm_substep_fwd(MpmHandle* h, const void* state_f, void* state_f1, const double* pose_f, const double* pose_f1,
-                    void* stream) {
+static int check_store(MpmHandle* h, const MpmGridStore* store, int32_t slot) {
+  if (!store) return MPM_OK;
+  if (slot < 0 || slot >= store->n_slots) return fail(h, MPM_E_INVALID, "grid store slot out of range");
+  if (store->capacity < 0 || !store->slot_start || !store->slot_count || !store->bump ||
+      (store->capacity > 0 && (!store->blocks || !store->block_ids)))
+    return fail(h, MPM_E_INVALID, "grid store has NULL buffers");
+  return check_aligned(h, store->blocks, "store->blocks", store->capacity == 0);
+}
+
+static int substep_fwd_impl(MpmHandle* h, const void* state_f, void* state_f1, const double* pose_f,
+                            const double* pose_f1, const MpmGridStore* store, int32_t slot, void* stream) {
   if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_substep_fwd: NULL handle");
   MPM_TRY(check_device(h));
   MPM_TRY(check_aligned(h, state_f, "state_f"));
@@ -387,24 +396,28 @@ int mpm_substep_fwd(MpmHandle* h, const void* state_f, void* state_f1, const dou
   if (state_f == state_f1) return fail(h, MPM_E_INVALID, "mpm_substep_fwd: state_f and state_f1 must differ");
   MPM_TRY(check_aligned(h, pose_f, "pose_f", h->n_tools == 0));
   MPM_TRY(check_aligned(h, pose_f1, "pose_f1", h->n_tools == 0));
+  MPM_TRY(check_store(h, store, slot));
   mpm::LaunchCtx L = ctx(h, stream);
   cudaError_t e;
   switch (h->p.precision) {
     case MPM_PREC_FP32:
-      e = mpm::launch_substep_fwd<float, float>(L, (const float*)state_f, (float*)state_f1, pose_f, pose_f1);
+      e = mpm::launch_substep_fwd<float, float>(L, (const float*)state_f, (float*)state_f1, pose_f, pose_f1, store,
+                                                slot);
       break;
     case MPM_PREC_FP32_SVD64:
-      e = mpm::launch_substep_fwd<float, double>(L, (const float*)state_f, (float*)state_f1, pose_f, pose_f1);
+      e = mpm::launch_substep_fwd<float, double>(L, (const float*)state_f, (float*)state_f1, pose_f, pose_f1, store,
+                                                 slot);
       break;
     default:
-      e = mpm::launch_substep_fwd<double, double>(L, (const double*)state_f, (double*)state_f1, pose_f, pose_f1);
+      e = mpm::launch_substep_fwd<double, double>(L, (const double*)state_f, (double*)state_f1, pose_f, pose_f1,
+                                                  store, slot);
   }
   return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_substep_fwd");
 }
 
-int mpm_substep_bwd(MpmHandle* h, const void* state_f, const void* g_state_f1, void* g_state_f,
-                    const double* pose_f, const double* pose_f1, double* g_pose_f, double* g_pose_f1,
-                    void* stream) {
+static int substep_bwd_impl(MpmHandle* h, const void* state_f, const void* g_state_f1, void* g_state_f,
+                            const double* pose_f, const double* pose_f1, double* g_pose_f, double* g_pose_f1,
+                            const MpmGridStore* store, int32_t slot, void* stream) {
   if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_substep_bwd: NULL handle");
   MPM_TRY(check_device(h));
   MPM_TRY(check_aligned(h, state_f, "state_f"));
@@ -416,22 +429,47 @@ int mpm_substep_bwd(MpmHandle* h, const void* state_f, const void* g_state_f1, v
   MPM_TRY(check_aligned(h, pose_f1, "pose_f1", nt));
   MPM_TRY(check_aligned(h, g_pose_f, "g_pose_f", nt));
   MPM_TRY(check_aligned(h, g_pose_f1, "g_pose_f1", nt));
+  MPM_TRY(check_store(h, store, slot));
   mpm::LaunchCtx L = ctx(h, stream);
   cudaError_t e;
   switch (h->p.precision) {
     case MPM_PREC_FP32:
       e = mpm::launch_substep_bwd<float, float>(L, (const float*)state_f, (const float*)g_state_f1, (float*)g_state_f,
-                                                pose_f, pose_f1, g_pose_f, g_pose_f1);
+                                                pose_f, pose_f1, g_pose_f, g_pose_f1, store, slot);
       break;
     case MPM_PREC_FP32_SVD64:
       e = mpm::launch_substep_bwd<float, double>(L, (const float*)state_f, (const float*)g_state_f1,
-                                                 (float*)g_state_f, pose_f, pose_f1, g_pose_f, g_pose_f1);
+                                                 (float*)g_state_f, pose_f, pose_f1, g_pose_f, g_pose_f1, store, slot);
       break;
     default:
       e = mpm::launch_substep_bwd<double, double>(L, (const double*)state_f, (const double*)g_state_f1,
-                                                  (double*)g_state_f, pose_f, pose_f1, g_pose_f, g_pose_f1);
+                                                  (double*)g_state_f, pose_f, pose_f1, g_pose_f, g_pose_f1, store,
+                                                  slot);
   }
   return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_substep_bwd");
+}
+
+int mpm_substep_fwd(MpmHandle* h, const void* state_f, void* state_f1, const double* pose_f, const double* pose_f1,
+                    void* stream) {
+  return substep_fwd_impl(h, state_f, state_f1, pose_f, pose_f1, nullptr, -1, stream);
+}
+int mpm_substep_fwd_store(MpmHandle* h, const void* state_f, void* state_f1, const double* pose_f,
+                          const double* pose_f1, const MpmGridStore* store, int32_t slot, void* stream) {
+  if (!store) return fail(h, MPM_E_INVALID, "mpm_substep_fwd_store: NULL store");
+  return substep_fwd_impl(h, state_f, state_f1, pose_f, pose_f1, store, slot, stream);
+}
+int mpm_substep_bwd(MpmHandle* h, const void* state_f, const void* g_state_f1, void* g_state_f,
+                    const double* pose_f, const double* pose_f1, double* g_pose_f, double* g_pose_f1,
+                    void* stream) {
+  return substep_bwd_impl(h, state_f, g_state_f1, g_state_f, pose_f, pose_f1, g_pose_f, g_pose_f1, nullptr, -1,
+                          stream);
+}
+int mpm_substep_bwd_store(MpmHandle* h, const void* state_f, const void* g_state_f1, void* g_state_f,
+                          const double* pose_f, const double* pose_f1, double* g_pose_f, double* g_pose_f1,
+                          const MpmGridStore* store, int32_t slot, void* stream) {
+  if (!store) return fail(h, MPM_E_INVALID, "mpm_substep_bwd_store: NULL store");
+  return substep_bwd_impl(h, state_f, g_state_f1, g_state_f, pose_f, pose_f1, g_pose_f, g_pose_f1, store, slot,
+                          stream);
 }
 
 int mpm_grid_mass(MpmHandle* h, const void* state, void* grid_m, void* stream) {

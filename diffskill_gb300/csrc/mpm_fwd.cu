@@ -40,22 +40,28 @@ static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs
 // Active blocks of frame st: clear flags, mark, compact, then zero the listed
 // blocks of grid a (and b if given).  Leaves the list in L.active and its
 // length at L.blockbuf[0..3].
+// ``saved`` (device, may be null): when it points at a slot start >= 0 the
+// list and grid a were restored from the grid store and are kept.
 template <typename T>
-cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* b) {
+cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* b,
+                           const MpmGridStore* store, int slot) {
   const int64_t total = (int64_t)c.n_scenes * c.NB3;
   int* counter = reinterpret_cast<int*>(L.blockbuf);
   unsigned char* flags = L.blockbuf + 16;
+  const int64_t* saved = store ? store->slot_start + slot : nullptr;
   MPM_MEMSET(L, L.blockbuf, blockbuf_bytes(c.n_scenes, c.n_grid));
+  if (store)
+    MPM_LAUNCH(L, MPM_K_CLEAR, k_store_restore<T>, (unsigned)(L.sm_count * 8), 256, *store, slot, L.active, counter, a);
   if (c.n_particles > 0)
-    MPM_LAUNCH(L, MPM_K_CLEAR, k_mark_blocks<T>, blocks_for(c.n_particles, 256), 256, c, st, L.pscene, flags);
-  MPM_LAUNCH(L, MPM_K_CLEAR, k_compact_blocks, blocks_for(total, 256), 256, flags, total, L.active, counter);
-  MPM_LAUNCH(L, MPM_K_CLEAR, k_clear_blocks<T>, (unsigned)(L.sm_count * 8), 256, L.active, counter, a, b);
+    MPM_LAUNCH(L, MPM_K_CLEAR, k_mark_blocks<T>, blocks_for(c.n_particles, 256), 256, c, st, L.pscene, flags, saved);
+  MPM_LAUNCH(L, MPM_K_CLEAR, k_compact_blocks, blocks_for(total, 256), 256, flags, total, L.active, counter, saved);
+  MPM_LAUNCH(L, MPM_K_CLEAR, k_clear_blocks<T>, (unsigned)(L.sm_count * 8), 256, L.active, counter, a, b, saved);
   return cudaGetLastError();
 }
 template cudaError_t prepare_blocks<float>(const LaunchCtx&, const Consts<float>&, const float*, Node<float>*,
-                                           Node<float>*);
+                                           Node<float>*, const MpmGridStore*, int);
 template cudaError_t prepare_blocks<double>(const LaunchCtx&, const Consts<double>&, const double*, Node<double>*,
-                                            Node<double>*);
+                                            Node<double>*, const MpmGridStore*, int);
 
 unsigned grid_blocks_launch(const LaunchCtx& L, int64_t total_blocks) {
   int64_t g = (int64_t)L.sm_count * 16;
@@ -64,15 +70,20 @@ unsigned grid_blocks_launch(const LaunchCtx& L, int64_t total_blocks) {
 
 template <typename T, typename S>
 cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const double* pose_f,
-                               const double* pose_f1) {
+                               const double* pose_f1, const MpmGridStore* store, int slot) {
   Consts<T> c = make_consts<T>(L);
   Node<T>* gin = (Node<T>*)L.grid_a;
   Node<T>* gout = (Node<T>*)L.grid_b;
   const int* counter = reinterpret_cast<const int*>(L.blockbuf);
-  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, (Node<T>*)nullptr);
+  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, (Node<T>*)nullptr, nullptr, -1);
   if (e != cudaSuccess) return e;
   if (c.n_particles > 0)
-    MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S>), blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gin);
+    MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S>), blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gin,
+               (const int64_t*)nullptr);
+  if (store) {
+    MPM_LAUNCH(L, MPM_K_CLEAR, k_store_reserve, 1, 1, *store, slot, counter);
+    MPM_LAUNCH(L, MPM_K_CLEAR, k_store_copy<T>, (unsigned)(L.sm_count * 8), 256, *store, slot, L.active, gin);
+  }
   MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3), 64, c, L.active,
              counter, gin, gout, L.tools, L.tool_off, pose_f, pose_f1);
   if (c.n_particles > 0)
@@ -199,8 +210,9 @@ template cudaError_t launch_tool_distance<float>(const LaunchCtx&, const int*, i
 template cudaError_t launch_tool_distance<double>(const LaunchCtx&, const int*, int, const double*, const double*,
                                                   double*);
 
-#define MPM_INST_FWD(T, S) \
-  template cudaError_t launch_substep_fwd<T, S>(const LaunchCtx&, const T*, T*, const double*, const double*);
+#define MPM_INST_FWD(T, S)                                                                             \
+  template cudaError_t launch_substep_fwd<T, S>(const LaunchCtx&, const T*, T*, const double*, const double*, \
+                                                const MpmGridStore*, int);
 MPM_INST_FWD(float, float)
 MPM_INST_FWD(float, double)
 MPM_INST_FWD(double, double)

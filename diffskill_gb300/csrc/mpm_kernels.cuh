@@ -350,7 +350,9 @@ MPM_DI MatConsts<S> mat_consts(const Consts<T>& c) {
 // ---------------------------------------------------------------------------
 template <typename T, typename S>
 __global__ void __launch_bounds__(128) k_p2g(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
-                                             const int* __restrict__ pscene, Node<T>* __restrict__ grid) {
+                                             const int* __restrict__ pscene, Node<T>* __restrict__ grid,
+                                             const int64_t* __restrict__ saved) {
+  if (saved && *saved >= 0) return;  // the grid of this substep was restored from the grid store
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = p < c.n_particles;  // every lane stays for the warp scan
   Stencil<T> s;
@@ -910,7 +912,9 @@ __global__ void __launch_bounds__(128) k_p2g_adj(Consts<T> c, const T* __restric
 template <typename T>
 __global__ void __launch_bounds__(256) k_mark_blocks(Consts<T> c, const T* __restrict__ st,
                                                      const int* __restrict__ pscene,
-                                                     unsigned char* __restrict__ flags) {
+                                                     unsigned char* __restrict__ flags,
+                                                     const int64_t* __restrict__ saved) {
+  if (saved && *saved >= 0) return;
   int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= c.n_particles) return;
   T x[3];
@@ -931,7 +935,9 @@ __global__ void __launch_bounds__(256) k_mark_blocks(Consts<T> c, const T* __res
 }
 // list of flagged blocks (warp-aggregated append; order is not significant)
 static __global__ void __launch_bounds__(256) k_compact_blocks(const unsigned char* __restrict__ flags, int64_t total,
-                                                        int* __restrict__ active, int* __restrict__ counter) {
+                                                               int* __restrict__ active, int* __restrict__ counter,
+                                                               const int64_t* __restrict__ saved) {
+  if (saved && *saved >= 0) return;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool f = i < total && flags[i] != 0;
   const unsigned m = __ballot_sync(0xffffffffu, f);
@@ -943,16 +949,62 @@ static __global__ void __launch_bounds__(256) k_compact_blocks(const unsigned ch
   base = __shfl_sync(0xffffffffu, base, leader);
   if (f) active[base + __popc(m & ((1u << lane) - 1u))] = (int)i;
 }
-// zero the listed blocks of one or two grids
+// zero the listed blocks of one or two grids (a is kept when restored from the store)
 template <typename T>
 __global__ void __launch_bounds__(256) k_clear_blocks(const int* __restrict__ active, const int* __restrict__ n_active,
-                                                      Node<T>* __restrict__ a, Node<T>* __restrict__ b) {
+                                                      Node<T>* __restrict__ a, Node<T>* __restrict__ b,
+                                                      const int64_t* __restrict__ saved) {
+  if (saved && *saved >= 0) a = nullptr;
+  if (!a && !b) return;
   const int64_t n = (int64_t)(*n_active) * 64;
   const Node<T> z = {T(0), T(0), T(0), T(0)};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t idx = (int64_t)active[i >> 6] * 64 + (i & 63);
-    a[idx] = z;
+    if (a) a[idx] = z;
     if (b) b[idx] = z;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// grid store: the forward grid of a substep (its active blocks) is kept so
+// the adjoint substep restores it instead of recomputing p2g
+// ---------------------------------------------------------------------------
+// one thread: reserve room for this substep's active blocks (bump allocator);
+// slot_start = -1 when the store is full (the adjoint then recomputes)
+static __global__ void k_store_reserve(MpmGridStore st, int slot, const int* __restrict__ n_active) {
+  const int n = *n_active;
+  const unsigned long long start = atomicAdd(st.bump, (unsigned long long)n);
+  const bool fits = start + (unsigned long long)n <= (unsigned long long)st.capacity;
+  st.slot_start[slot] = fits ? (int64_t)start : -1;
+  st.slot_count[slot] = fits ? n : 0;
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_store_copy(MpmGridStore st, int slot, const int* __restrict__ active,
+                                                    const Node<T>* __restrict__ grid) {
+  const int64_t start = st.slot_start[slot];
+  if (start < 0) return;
+  const int64_t n = (int64_t)st.slot_count[slot] * 64;
+  Node<T>* dst = reinterpret_cast<Node<T>*>(st.blocks);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int blk = active[i >> 6];
+    dst[(start << 6) + i] = grid[(int64_t)blk * 64 + (i & 63)];
+    if ((i & 63) == 0) st.block_ids[start + (i >> 6)] = blk;
+  }
+}
+// restore the active list and the grid blocks of a stored substep
+template <typename T>
+__global__ void __launch_bounds__(256) k_store_restore(MpmGridStore st, int slot, int* __restrict__ active,
+                                                       int* __restrict__ n_active, Node<T>* __restrict__ grid) {
+  const int64_t start = st.slot_start[slot];
+  if (start < 0) return;
+  const int cnt = st.slot_count[slot];
+  if (blockIdx.x == 0 && threadIdx.x == 0) *n_active = cnt;
+  const Node<T>* src = reinterpret_cast<const Node<T>*>(st.blocks);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)cnt * 64;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int blk = st.block_ids[start + (i >> 6)];
+    if ((i & 63) == 0) active[i >> 6] = blk;
+    grid[(int64_t)blk * 64 + (i & 63)] = src[(start << 6) + i];
   }
 }
 

@@ -171,13 +171,25 @@ class MpmEngine:
         _lib.check(self.lib.mpm_tools_action_bwd(self.h, _ptr(vel), _ptr(pose), _ptr(g_pose), _ptr(g_action),
                                                  self.n_sub, _stream()), self.h, "mpm_tools_action_bwd")
 
-    def substep(self, st0, st1, pose_f, pose_f1) -> None:
-        _lib.check(self.lib.mpm_substep_fwd(self.h, _ptr(st0), _ptr(st1), _ptr(pose_f), _ptr(pose_f1), _stream()),
-                   self.h, "mpm_substep_fwd")
+    def substep(self, st0, st1, pose_f, pose_f1, store: "GridStore" = None, slot: int = -1) -> None:
+        if store is None:
+            _lib.check(self.lib.mpm_substep_fwd(self.h, _ptr(st0), _ptr(st1), _ptr(pose_f), _ptr(pose_f1),
+                                                _stream()), self.h, "mpm_substep_fwd")
+        else:
+            _lib.check(self.lib.mpm_substep_fwd_store(self.h, _ptr(st0), _ptr(st1), _ptr(pose_f), _ptr(pose_f1),
+                                                      ctypes.byref(store.struct), slot, _stream()), self.h,
+                       "mpm_substep_fwd_store")
 
-    def substep_bwd(self, st0, g1, g0, pose_f, pose_f1, gp_f, gp_f1) -> None:
-        _lib.check(self.lib.mpm_substep_bwd(self.h, _ptr(st0), _ptr(g1), _ptr(g0), _ptr(pose_f), _ptr(pose_f1),
-                                            _ptr(gp_f), _ptr(gp_f1), _stream()), self.h, "mpm_substep_bwd")
+    def substep_bwd(self, st0, g1, g0, pose_f, pose_f1, gp_f, gp_f1, store: "GridStore" = None,
+                    slot: int = -1) -> None:
+        if store is None:
+            _lib.check(self.lib.mpm_substep_bwd(self.h, _ptr(st0), _ptr(g1), _ptr(g0), _ptr(pose_f), _ptr(pose_f1),
+                                                _ptr(gp_f), _ptr(gp_f1), _stream()), self.h, "mpm_substep_bwd")
+        else:
+            _lib.check(self.lib.mpm_substep_bwd_store(self.h, _ptr(st0), _ptr(g1), _ptr(g0), _ptr(pose_f),
+                                                      _ptr(pose_f1), _ptr(gp_f), _ptr(gp_f1),
+                                                      ctypes.byref(store.struct), slot, _stream()), self.h,
+                       "mpm_substep_bwd_store")
 
     def grid_mass(self, st: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         if out is None:
@@ -259,6 +271,44 @@ class MpmEngine:
         return slice(int(self.offsets[s]), int(self.offsets[s + 1]))
 
 
+class GridStore:
+    """Caller-owned arena of forward-grid blocks (``MpmGridStore`` of the C ABI).
+
+    Substeps whose forward grid is stored skip the p2g recompute in their
+    adjoint; a substep that does not fit is recomputed (same result).
+    """
+
+    def __init__(self, eng: MpmEngine, n_slots: int, capacity_blocks: int):
+        dev = eng.device
+        self.capacity = int(max(capacity_blocks, 0))
+        self.blocks = torch.empty((max(self.capacity, 1), 64, 4), dtype=eng.dtype, device=dev)
+        self.block_ids = torch.empty(max(self.capacity, 1), dtype=torch.int32, device=dev)
+        self.slot_start = torch.full((n_slots,), -1, dtype=torch.int64, device=dev)
+        self.slot_count = torch.zeros(n_slots, dtype=torch.int32, device=dev)
+        self.bump = torch.zeros(1, dtype=torch.int64, device=dev)
+        st = _lib.MpmGridStore()
+        st.blocks = self.blocks.data_ptr()
+        st.block_ids = self.block_ids.data_ptr()
+        st.slot_start = self.slot_start.data_ptr()
+        st.slot_count = self.slot_count.data_ptr()
+        st.bump = self.bump.data_ptr()
+        st.capacity = self.capacity
+        st.n_slots = int(n_slots)
+        self.struct = st
+
+    def reset(self) -> None:
+        """Forget every slot (device-side; capturable)."""
+        self.bump.zero_()
+        self.slot_start.fill_(-1)
+
+    def bytes(self) -> int:
+        return sum(t.numel() * t.element_size() for t in (self.blocks, self.block_ids, self.slot_start,
+                                                           self.slot_count, self.bump))
+
+    def stored_slots(self) -> int:
+        return int((self.slot_start >= 0).sum())
+
+
 class Horizon:
     """Device buffers and the forward/backward sweep over ``n_actions`` actions.
 
@@ -267,7 +317,8 @@ class Horizon:
     of k substeps from its checkpoint before running its adjoint.
     """
 
-    def __init__(self, eng: MpmEngine, n_actions: int, ckpt_every: int = 10):
+    def __init__(self, eng: MpmEngine, n_actions: int, ckpt_every: int = 10, store_grids: bool = True,
+                 store_budget_bytes: Optional[int] = None):
         self.eng = eng
         self.A = int(n_actions)
         self.F = self.A * eng.n_sub
@@ -292,10 +343,21 @@ class Horizon:
         self.movable = torch.tensor([float(t.action.dim > 0) for t in eng.tool_cfgs] or [0.0],
                                     dtype=torch.float64, device=dev)[:eng.T]
         self.tool_scene = torch.tensor(eng.tool_scene or [0], dtype=torch.long, device=dev)[:eng.T]
+        # forward-grid store: every substep when every frame is kept (k == 1), else one segment
+        self.store = None
+        if store_grids:
+            n_slots = self.F if k == 1 else k
+            block_bytes = 64 * 4 * (8 if dt == torch.float64 else 4) + 4
+            if store_budget_bytes is None:
+                free, _ = torch.cuda.mem_get_info(dev)
+                store_budget_bytes = free // 4
+            worst = n_slots * eng.S * (eng.n_grid // 4) ** 3
+            self.store = GridStore(eng, n_slots, min(worst, store_budget_bytes // block_bytes))
 
     def bytes(self) -> int:
         return sum(t.numel() * t.element_size() for t in
-                   (self.ckpt, self.seg, self.pose, self.vel, self.g, self.gm, self.g_gm, self.g_pose))
+                   (self.ckpt, self.seg, self.pose, self.vel, self.g, self.gm, self.g_gm, self.g_pose)) + (
+                       self.store.bytes() if self.store is not None else 0)
 
     @property
     def final(self) -> torch.Tensor:
@@ -310,13 +372,16 @@ class Horizon:
             self.acts.copy_(actions)
             for s in range(self.A):
                 eng.tools_action(self.acts[s], self.vel[s * n], self.pose[s * n])
+        store = self.store if (self.store is not None and self.k == 1) else None
+        if store is not None:
+            store.reset()
         cur = self.ckpt[0]
         for f in range(self.F):
             if (f + 1) % self.k == 0:
                 nxt = self.ckpt[(f + 1) // self.k]
             else:
                 nxt = self.seg[(f + 1) % 2]
-            eng.substep(cur, nxt, self.pose[f], self.pose[f + 1])
+            eng.substep(cur, nxt, self.pose[f], self.pose[f + 1], store, f)
             cur = nxt
 
     def loss(self, targets: torch.Tensor, density_weight: float = 1.0, contact_weight: float = 0.0,
@@ -359,16 +424,21 @@ class Horizon:
         self._loss_grad_ready = False
         nxt = self.g[1]
         self.g_act.zero_()
+        store = self.store
         for c in range(self.F // k - 1, -1, -1):
             frames = [self.ckpt[c]]
+            if store is not None and k > 1:
+                store.reset()  # this segment's substeps are stored while they are recomputed
             for i in range(1, k):
                 dst = self.seg[i]
-                eng.substep(frames[-1], dst, self.pose[c * k + i - 1], self.pose[c * k + i])
+                eng.substep(frames[-1], dst, self.pose[c * k + i - 1], self.pose[c * k + i], store,
+                            i - 1 if store is not None else -1)
                 frames.append(dst)
             for i in range(k - 1, -1, -1):
                 f = c * k + i
+                slot = -1 if store is None else (f if k == 1 else i)
                 eng.substep_bwd(frames[i], cur, nxt, self.pose[f], self.pose[f + 1], self.g_pose[f],
-                                self.g_pose[f + 1])
+                                self.g_pose[f + 1], store if slot >= 0 else None, slot)
                 cur, nxt = nxt, cur
         if eng.T:
             for s in range(self.A - 1, -1, -1):

@@ -91,6 +91,23 @@ typedef struct MpmToolDesc {
   double action_scale[7];
 } MpmToolDesc;
 
+/* Grid store (caller-owned device buffers): the forward grid of a substep,
+ * i.e. its active 4x4x4-node blocks, kept so the adjoint substep restores it
+ * instead of recomputing p2g.  Slots are filled by a device-side bump
+ * allocator; a substep that does not fit gets slot_start = -1 and its adjoint
+ * recomputes the grid, so results never depend on the capacity.  Zero *bump
+ * (and set slot_start to -1) before reusing slots. */
+typedef struct MpmGridStore {
+  void* blocks;                 /* real[capacity][64][4] */
+  int32_t* block_ids;           /* [capacity] global block id of each stored block */
+  int64_t* slot_start;          /* [n_slots] first stored block of the slot, -1 = not stored */
+  int32_t* slot_count;          /* [n_slots] */
+  unsigned long long* bump;     /* [1] blocks handed out so far */
+  int64_t capacity;             /* blocks */
+  int32_t n_slots;
+  int32_t reserved;
+} MpmGridStore;
+
 typedef struct MpmHandle MpmHandle;
 
 const char* mpm_version(void);
@@ -133,6 +150,17 @@ int mpm_substep_fwd(MpmHandle* h, const void* state_f, void* state_f1, const dou
 int mpm_substep_bwd(MpmHandle* h, const void* state_f, const void* g_state_f1, void* g_state_f,
                     const double* pose_f, const double* pose_f1, double* g_pose_f, double* g_pose_f1,
                     void* stream);
+
+/* mpm_substep_fwd that also keeps the substep's forward grid in store slot
+ * `slot` (no counterpart in the reference, whose substep_grad always
+ * recomputes the grid, mpm_simulator.py:327-333). */
+int mpm_substep_fwd_store(MpmHandle* h, const void* state_f, void* state_f1, const double* pose_f,
+                          const double* pose_f1, const MpmGridStore* store, int32_t slot, void* stream);
+/* mpm_substep_bwd that restores the forward grid from store slot `slot` when
+ * it was stored, and recomputes it otherwise. */
+int mpm_substep_bwd_store(MpmHandle* h, const void* state_f, const void* g_state_f1, void* g_state_f,
+                          const double* pose_f, const double* pose_f1, double* g_pose_f, double* g_pose_f1,
+                          const MpmGridStore* store, int32_t slot, void* stream);
 
 /* compute_grid_m_kernel on a cleared grid (mpm_simulator.py:456-471).
  * grid_m: real[n_scenes][n_grid^3] written. */

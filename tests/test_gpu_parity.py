@@ -277,3 +277,28 @@ def test_sorted_particles_warp_aggregated_scatter_matches_oracle(gpu_lib, prec, 
     ref_loss, ref_grad = Oracle(sc.sim, sc.tools).loss_and_grad(sc.x0, sc.actions, sc.target)
     assert abs(loss - ref_loss) / abs(ref_loss) < loss_tol, (loss, ref_loss)
     assert rel_err(grad, ref_grad) < grad_tol, (grad, ref_grad)
+
+
+@pytest.mark.parametrize("k", [1, 10])
+def test_grid_store_restore_equals_recompute(gpu_lib, k):
+    """Restoring the stored forward grid in the adjoint gives the recompute
+    path's loss and gradients, also when the store fills up part way."""
+    sc = small_scene(n=4000, n_actions=2, substeps=50, tools=[all_tools()[1], all_tools()[2]], precision="fp64")
+    eng = make_engine(sc)
+    out = []
+    for store, budget in ((False, None), (True, None), (True, 64 * 1037 * 3)):
+        hz = Horizon(eng, sc.n_actions, ckpt_every=k, store_grids=store, store_budget_bytes=budget)
+        hz.forward(eng.init_state([sc.x0]), eng.expand_actions([sc.actions]))
+        loss = float(hz.loss(eng.targets([sc.target])).sum())
+        g = eng.collapse_action_grad(hz.backward())[0].cpu().numpy()
+        torch.cuda.synchronize()
+        if store:
+            n_stored = hz.store.stored_slots()
+            assert n_stored > 0
+            if budget is not None:
+                assert n_stored < hz.store.slot_start.numel()  # partly stored, partly recomputed
+        out.append((loss, g))
+    (l0, g0) = out[0]
+    for l, g in out[1:]:
+        assert abs(l - l0) <= 1e-12 * abs(l0)
+        assert rel_err(g, g0) < 1e-9
