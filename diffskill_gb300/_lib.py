@@ -57,10 +57,10 @@ SIGNATURES = {
     "mpm_tools_action": (_i32, [_c_p, _c_p, _c_p, _c_p, _i32, _c_p]),
     "mpm_tools_action_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _i32, _c_p]),
     "mpm_substep_fwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
-    "mpm_substep_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
+    "mpm_substep_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_substep_fwd_store": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, ctypes.POINTER(MpmGridStore), _i32, _c_p]),
-    "mpm_substep_bwd_store": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, ctypes.POINTER(MpmGridStore),
-                                     _i32, _c_p]),
+    "mpm_substep_bwd_store": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p,
+                                     ctypes.POINTER(MpmGridStore), _i32, _c_p]),
     "mpm_grid_mass": (_i32, [_c_p, _c_p, _c_p, _c_p]),
     "mpm_grid_mass_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_density_l1": (_i32, [_c_p, _c_p, _c_p, _f64, _c_p, _c_p, _c_p]),

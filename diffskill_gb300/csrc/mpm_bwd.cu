@@ -15,9 +15,9 @@ unsigned grid_blocks_launch(const LaunchCtx& L, int64_t total_blocks);
 static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 template <typename T, typename S>
-cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* g1, T* g0, const double* pose_f,
-                               const double* pose_f1, double* g_pose_f, double* g_pose_f1, const MpmGridStore* store,
-                               int slot) {
+cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* st1, const T* g1, T* g0,
+                               const double* pose_f, const double* pose_f1, double* g_pose_f, double* g_pose_f1,
+                               const MpmGridStore* store, int slot) {
   Consts<T> c = make_consts<T>(L);
   Node<T>* gin = (Node<T>*)L.grid_a;
   Node<T>* gout = (Node<T>*)L.grid_b;
@@ -35,7 +35,7 @@ cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* g1, T*
   MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, gb, 64, c, L.active, counter, gin, gout, L.tools, L.tool_off, pose_f,
              pose_f1);
   if (c.n_particles > 0)
-    MPM_LAUNCH(L, MPM_K_G2P_ADJ, k_g2p_adj<T>, pb, 128, c, st0, g1, g0, L.pscene, gout, g_gout);
+    MPM_LAUNCH(L, MPM_K_G2P_ADJ, k_g2p_adj<T>, pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
   MPM_LAUNCH(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, gb, 64, c, L.active, counter, gin, g_gout, g_gin, L.tools,
              L.tool_off, pose_f, pose_f1, g_pose_f, g_pose_f1);
   if (c.n_particles > 0)
@@ -164,7 +164,7 @@ template cudaError_t launch_tool_distance_bwd<double>(const LaunchCtx&, const in
                                                       const double*, double*, double*);
 
 #define MPM_INST_BWD(T, S)                                                                                  \
-  template cudaError_t launch_substep_bwd<T, S>(const LaunchCtx&, const T*, const T*, T*, const double*, \
+  template cudaError_t launch_substep_bwd<T, S>(const LaunchCtx&, const T*, const T*, const T*, T*, const double*, \
                                                 const double*, double*, double*, const MpmGridStore*, int);
 MPM_INST_BWD(float, float)
 MPM_INST_BWD(float, double)

@@ -415,12 +415,14 @@ static int substep_fwd_impl(MpmHandle* h, const void* state_f, void* state_f1, c
   return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_substep_fwd");
 }
 
-static int substep_bwd_impl(MpmHandle* h, const void* state_f, const void* g_state_f1, void* g_state_f,
+static int substep_bwd_impl(MpmHandle* h, const void* state_f, const void* state_f1, const void* g_state_f1,
+                            void* g_state_f,
                             const double* pose_f, const double* pose_f1, double* g_pose_f, double* g_pose_f1,
                             const MpmGridStore* store, int32_t slot, void* stream) {
   if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_substep_bwd: NULL handle");
   MPM_TRY(check_device(h));
   MPM_TRY(check_aligned(h, state_f, "state_f"));
+  MPM_TRY(check_aligned(h, state_f1, "state_f1", true));
   MPM_TRY(check_aligned(h, g_state_f1, "g_state_f1"));
   MPM_TRY(check_aligned(h, g_state_f, "g_state_f"));
   if (g_state_f == g_state_f1) return fail(h, MPM_E_INVALID, "mpm_substep_bwd: g_state_f and g_state_f1 must differ");
@@ -434,17 +436,19 @@ static int substep_bwd_impl(MpmHandle* h, const void* state_f, const void* g_sta
   cudaError_t e;
   switch (h->p.precision) {
     case MPM_PREC_FP32:
-      e = mpm::launch_substep_bwd<float, float>(L, (const float*)state_f, (const float*)g_state_f1, (float*)g_state_f,
-                                                pose_f, pose_f1, g_pose_f, g_pose_f1, store, slot);
+      e = mpm::launch_substep_bwd<float, float>(L, (const float*)state_f, (const float*)state_f1,
+                                                (const float*)g_state_f1, (float*)g_state_f, pose_f, pose_f1,
+                                                g_pose_f, g_pose_f1, store, slot);
       break;
     case MPM_PREC_FP32_SVD64:
-      e = mpm::launch_substep_bwd<float, double>(L, (const float*)state_f, (const float*)g_state_f1,
-                                                 (float*)g_state_f, pose_f, pose_f1, g_pose_f, g_pose_f1, store, slot);
+      e = mpm::launch_substep_bwd<float, double>(L, (const float*)state_f, (const float*)state_f1,
+                                                 (const float*)g_state_f1, (float*)g_state_f, pose_f, pose_f1,
+                                                 g_pose_f, g_pose_f1, store, slot);
       break;
     default:
-      e = mpm::launch_substep_bwd<double, double>(L, (const double*)state_f, (const double*)g_state_f1,
-                                                  (double*)g_state_f, pose_f, pose_f1, g_pose_f, g_pose_f1, store,
-                                                  slot);
+      e = mpm::launch_substep_bwd<double, double>(L, (const double*)state_f, (const double*)state_f1,
+                                                  (const double*)g_state_f1, (double*)g_state_f, pose_f, pose_f1,
+                                                  g_pose_f, g_pose_f1, store, slot);
   }
   return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_substep_bwd");
 }
@@ -458,18 +462,18 @@ int mpm_substep_fwd_store(MpmHandle* h, const void* state_f, void* state_f1, con
   if (!store) return fail(h, MPM_E_INVALID, "mpm_substep_fwd_store: NULL store");
   return substep_fwd_impl(h, state_f, state_f1, pose_f, pose_f1, store, slot, stream);
 }
-int mpm_substep_bwd(MpmHandle* h, const void* state_f, const void* g_state_f1, void* g_state_f,
-                    const double* pose_f, const double* pose_f1, double* g_pose_f, double* g_pose_f1,
-                    void* stream) {
-  return substep_bwd_impl(h, state_f, g_state_f1, g_state_f, pose_f, pose_f1, g_pose_f, g_pose_f1, nullptr, -1,
-                          stream);
+int mpm_substep_bwd(MpmHandle* h, const void* state_f, const void* state_f1, const void* g_state_f1,
+                    void* g_state_f, const double* pose_f, const double* pose_f1, double* g_pose_f,
+                    double* g_pose_f1, void* stream) {
+  return substep_bwd_impl(h, state_f, state_f1, g_state_f1, g_state_f, pose_f, pose_f1, g_pose_f, g_pose_f1,
+                          nullptr, -1, stream);
 }
-int mpm_substep_bwd_store(MpmHandle* h, const void* state_f, const void* g_state_f1, void* g_state_f,
-                          const double* pose_f, const double* pose_f1, double* g_pose_f, double* g_pose_f1,
-                          const MpmGridStore* store, int32_t slot, void* stream) {
+int mpm_substep_bwd_store(MpmHandle* h, const void* state_f, const void* state_f1, const void* g_state_f1,
+                          void* g_state_f, const double* pose_f, const double* pose_f1, double* g_pose_f,
+                          double* g_pose_f1, const MpmGridStore* store, int32_t slot, void* stream) {
   if (!store) return fail(h, MPM_E_INVALID, "mpm_substep_bwd_store: NULL store");
-  return substep_bwd_impl(h, state_f, g_state_f1, g_state_f, pose_f, pose_f1, g_pose_f, g_pose_f1, store, slot,
-                          stream);
+  return substep_bwd_impl(h, state_f, state_f1, g_state_f1, g_state_f, pose_f, pose_f1, g_pose_f, g_pose_f1, store,
+                          slot, stream);
 }
 
 int mpm_grid_mass(MpmHandle* h, const void* state, void* grid_m, void* stream) {

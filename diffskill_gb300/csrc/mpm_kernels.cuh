@@ -179,6 +179,18 @@ MPM_DI void zero_stencil(Stencil<T>& s) {
     for (int k = 0; k < 3; ++k) s.w[k][d] = T(0);
   }
 }
+// a[i] for a runtime i in 0..2 without local memory
+template <typename T>
+MPM_DI T sel3(T a0, T a1, T a2, int i) {
+  return i == 0 ? a0 : (i == 1 ? a1 : a2);
+}
+template <typename T>
+MPM_DI void add3(T& a0, T& a1, T& a2, int i, T v) {
+  a0 += i == 0 ? v : T(0);
+  a1 += i == 1 ? v : T(0);
+  a2 += i == 2 ? v : T(0);
+}
+
 template <typename T>
 MPM_DI long long cell_key(const Consts<T>& c, int scene, const Stencil<T>& s) {
   return (long long)scene * c.G + ((long long)s.base[0] * c.n_grid + s.base[1]) * c.n_grid + s.base[2];
@@ -396,14 +408,17 @@ __global__ void __launch_bounds__(128) k_p2g(Consts<T> c, const T* __restrict__ 
   const WarpSeg seg = warp_segments(ok ? cell_key(c, scene, s) : -1 - (long long)(threadIdx.x & 31));
   Node<T>* g = grid + (int64_t)scene * c.G;
   const StencilAddr A = stencil_addr(c, s);
-#pragma unroll
-  for (int ox = 0; ox < 3; ++ox)
+#pragma unroll 1
+  for (int ox = 0; ox < 3; ++ox) {
+    const T wx = sel3(s.w[0][0], s.w[1][0], s.w[2][0], ox);
+    const int ax = sel3(A.ax[0], A.ax[1], A.ax[2], ox);
+    const T dpx = (T(ox) - s.fx[0]) * c.dx;
 #pragma unroll
     for (int oy = 0; oy < 3; ++oy)
 #pragma unroll
       for (int oz = 0; oz < 3; ++oz) {
-        const T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
-        const T dp[3] = {(T(ox) - s.fx[0]) * c.dx, (T(oy) - s.fx[1]) * c.dx, (T(oz) - s.fx[2]) * c.dx};
+        const T wgt = wx * s.w[oy][1] * s.w[oz][2];
+        const T dp[3] = {dpx, (T(oy) - s.fx[1]) * c.dx, (T(oz) - s.fx[2]) * c.dx};
         T mv[4];
 #pragma unroll
         for (int k = 0; k < 3; ++k)
@@ -413,8 +428,9 @@ __global__ void __launch_bounds__(128) k_p2g(Consts<T> c, const T* __restrict__ 
 #pragma unroll
           for (int k = 0; k < 4; ++k) mv[k] = seg_scan(mv[k], seg);
         }
-        if (ok && seg.tail) atomic_add_node(g + A.at(ox, oy, oz), mv[0], mv[1], mv[2], mv[3]);
+        if (ok && seg.tail) atomic_add_node(g + ax + A.ay[oy] + A.az[oz], mv[0], mv[1], mv[2], mv[3]);
       }
+  }
 }
 
 // Per-CTA tool table of one scene in shared memory.
@@ -636,10 +652,13 @@ __global__ void __launch_bounds__(128) k_g2p(Consts<T> c, const T* __restrict__ 
 // adjoint kernels
 // ---------------------------------------------------------------------------
 // g2p.grad: writes the x rows of g0 (partial) and scatters into g_grid
+// st1 (frame f+1, may be null): its v rows are the g2p output, so the clamp
+// mask needs no second gather of the grid.
 template <typename T>
-__global__ void __launch_bounds__(128) k_g2p_adj(Consts<T> c, const T* __restrict__ st, const T* __restrict__ g1,
-                                                 T* __restrict__ g0, const int* __restrict__ pscene,
-                                                 const Node<T>* __restrict__ grid, Node<T>* __restrict__ g_grid) {
+__global__ void __launch_bounds__(128) k_g2p_adj(Consts<T> c, const T* __restrict__ st, const T* __restrict__ st1,
+                                                 const T* __restrict__ g1, T* __restrict__ g0,
+                                                 const int* __restrict__ pscene, const Node<T>* __restrict__ grid,
+                                                 Node<T>* __restrict__ g_grid) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = p < c.n_particles;  // every lane stays for the warp scan
   Stencil<T> s;
@@ -667,18 +686,22 @@ __global__ void __launch_bounds__(128) k_g2p_adj(Consts<T> c, const T* __restric
 #pragma unroll
   for (int k = 0; k < 9; ++k) gC[k] = T(0);
   if (ok) {
+    if (st1) {
+      load_row(st1, c.ld, p, 3, 3, nv);
+    } else {
 #pragma unroll
-    for (int ox = 0; ox < 3; ++ox)
+      for (int ox = 0; ox < 3; ++ox)
 #pragma unroll
-      for (int oy = 0; oy < 3; ++oy)
+        for (int oy = 0; oy < 3; ++oy)
 #pragma unroll
-        for (int oz = 0; oz < 3; ++oz) {
-          T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
-          Node<T> n = g[A.at(ox, oy, oz)];
-          nv[0] += wgt * n.x;
-          nv[1] += wgt * n.y;
-          nv[2] += wgt * n.z;
-        }
+          for (int oz = 0; oz < 3; ++oz) {
+            T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
+            Node<T> n = g[A.at(ox, oy, oz)];
+            nv[0] += wgt * n.x;
+            nv[1] += wgt * n.y;
+            nv[2] += wgt * n.z;
+          }
+    }
     T gx1[3];
     load_row(g1, c.ld, p, 0, 3, gx1);
     load_row(g1, c.ld, p, 3, 3, gnv);
@@ -701,14 +724,18 @@ __global__ void __launch_bounds__(128) k_g2p_adj(Consts<T> c, const T* __restric
 #pragma unroll
     for (int b = 0; b < 3; ++b) gw[a][b] = T(0);
   T gfx[3] = {T(0), T(0), T(0)};
-#pragma unroll
-  for (int ox = 0; ox < 3; ++ox)
+#pragma unroll 1
+  for (int ox = 0; ox < 3; ++ox) {
+    const T wx = sel3(s.w[0][0], s.w[1][0], s.w[2][0], ox);
+    const int ax = sel3(A.ax[0], A.ax[1], A.ax[2], ox);
+    const T dpx = T(ox) - s.fx[0];
+    T gwx = T(0);
 #pragma unroll
     for (int oy = 0; oy < 3; ++oy)
 #pragma unroll
       for (int oz = 0; oz < 3; ++oz) {
-        const T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
-        const T dp[3] = {T(ox) - s.fx[0], T(oy) - s.fx[1], T(oz) - s.fx[2]};
+        const T wgt = wx * s.w[oy][1] * s.w[oz][2];
+        const T dp[3] = {dpx, T(oy) - s.fx[1], T(oz) - s.fx[2]};
         T gCd[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) gCd[i] = gC[3 * i] * dp[0] + gC[3 * i + 1] * dp[1] + gC[3 * i + 2] * dp[2];
@@ -718,18 +745,21 @@ __global__ void __launch_bounds__(128) k_g2p_adj(Consts<T> c, const T* __restric
           for (int k = 0; k < 3; ++k) sc3[k] = seg_scan(sc3[k], seg);
         }
         if (ok) {
-          if (seg.tail) atomic_add_node3(gg + A.at(ox, oy, oz), sc3[0], sc3[1], sc3[2]);
-          Node<T> n = g[A.at(ox, oy, oz)];
+          const int64_t a = ax + A.ay[oy] + A.az[oz];
+          if (seg.tail) atomic_add_node3(gg + a, sc3[0], sc3[1], sc3[2]);
+          Node<T> n = g[a];
           const T gv[3] = {n.x, n.y, n.z};
           T g_wgt = dot3(gv, gnv) + k4 * dot3(gv, gCd);
 #pragma unroll
           for (int j = 0; j < 3; ++j)
             gfx[j] -= k4 * wgt * (gC[j] * gv[0] + gC[3 + j] * gv[1] + gC[6 + j] * gv[2]);
-          gw[ox][0] += g_wgt * s.w[oy][1] * s.w[oz][2];
-          gw[oy][1] += g_wgt * s.w[ox][0] * s.w[oz][2];
-          gw[oz][2] += g_wgt * s.w[ox][0] * s.w[oy][1];
+          gwx += g_wgt * s.w[oy][1] * s.w[oz][2];
+          gw[oy][1] += g_wgt * wx * s.w[oz][2];
+          gw[oz][2] += g_wgt * wx * s.w[oy][1];
         }
       }
+    add3(gw[0][0], gw[1][0], gw[2][0], ox, gwx);
+  }
   if (ok) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) {

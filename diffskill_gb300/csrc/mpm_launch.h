@@ -74,7 +74,7 @@ template <typename T, typename S>
 cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const double* pose_f,
                                const double* pose_f1, const MpmGridStore* store = nullptr, int slot = -1);
 template <typename T, typename S>
-cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* g1, T* g0, const double* pose_f,
+cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* st1, const T* g1, T* g0, const double* pose_f,
                                const double* pose_f1, double* g_pose_f, double* g_pose_f1,
                                const MpmGridStore* store = nullptr, int slot = -1);
 template <typename T>

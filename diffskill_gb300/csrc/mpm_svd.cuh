@@ -26,14 +26,29 @@ struct SvdIters<double> {
   static constexpr double tol = 1e-32;
 };
 
+// rotation tangent t = sgn(theta) / (|theta| + sqrt(theta^2 + 1)) and cosine c;
+// FP32 uses the fast reciprocal and rsqrt (c and s = t c come from the same
+// rsqrt, so the rotation stays orthogonal to rounding)
+MPM_DI void rot_tc(double theta, double& t, double& c) {
+  t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+  c = 1.0 / sqrt(t * t + 1.0);
+}
+MPM_DI void rot_tc(float theta, float& t, float& c) {
+  const float at = fabsf(theta);
+  // for huge |theta|, t ~ 1/(2 theta) (avoids theta^2 overflow)
+  const float den = at < 1e18f ? at + sqrtf(fmaf(theta, theta, 1.0f)) : 2.0f * at;
+  t = copysignf(__frcp_rn(den), theta);
+  c = rsqrtf(fmaf(t, t, 1.0f));
+}
+
 // one Jacobi rotation zeroing s_pq of the symmetric matrix held as
 // (s_pp, s_qq, s_pq, s_rp, s_rq); V columns p, q rotated alongside
 template <typename T>
 MPM_DI void jacobi_rot(T& app, T& aqq, T& apq, T& arp, T& arq, T* V, int p, int q) {
   if (apq == T(0)) return;
   T theta = (aqq - app) / (T(2) * apq);
-  T t = (theta >= T(0) ? T(1) : T(-1)) / (mabs(theta) + msqrt(theta * theta + T(1)));
-  T c = T(1) / msqrt(t * t + T(1));
+  T t, c;
+  rot_tc(theta, t, c);
   T s = t * c;
   app = app - t * apq;
   aqq = aqq + t * apq;

@@ -181,12 +181,14 @@ class MpmEngine:
                        "mpm_substep_fwd_store")
 
     def substep_bwd(self, st0, g1, g0, pose_f, pose_f1, gp_f, gp_f1, store: "GridStore" = None,
-                    slot: int = -1) -> None:
+                    slot: int = -1, st1: Optional[torch.Tensor] = None) -> None:
+        """Adjoint of one substep; ``st1`` (frame f+1 from the forward) is optional."""
         if store is None:
-            _lib.check(self.lib.mpm_substep_bwd(self.h, _ptr(st0), _ptr(g1), _ptr(g0), _ptr(pose_f), _ptr(pose_f1),
-                                                _ptr(gp_f), _ptr(gp_f1), _stream()), self.h, "mpm_substep_bwd")
+            _lib.check(self.lib.mpm_substep_bwd(self.h, _ptr(st0), _ptr(st1), _ptr(g1), _ptr(g0), _ptr(pose_f),
+                                                _ptr(pose_f1), _ptr(gp_f), _ptr(gp_f1), _stream()), self.h,
+                       "mpm_substep_bwd")
         else:
-            _lib.check(self.lib.mpm_substep_bwd_store(self.h, _ptr(st0), _ptr(g1), _ptr(g0), _ptr(pose_f),
+            _lib.check(self.lib.mpm_substep_bwd_store(self.h, _ptr(st0), _ptr(st1), _ptr(g1), _ptr(g0), _ptr(pose_f),
                                                       _ptr(pose_f1), _ptr(gp_f), _ptr(gp_f1),
                                                       ctypes.byref(store.struct), slot, _stream()), self.h,
                        "mpm_substep_bwd_store")
@@ -437,8 +439,9 @@ class Horizon:
             for i in range(k - 1, -1, -1):
                 f = c * k + i
                 slot = -1 if store is None else (f if k == 1 else i)
+                st1 = frames[i + 1] if i + 1 < k else self.ckpt[c + 1]
                 eng.substep_bwd(frames[i], cur, nxt, self.pose[f], self.pose[f + 1], self.g_pose[f],
-                                self.g_pose[f + 1], store if slot >= 0 else None, slot)
+                                self.g_pose[f + 1], store if slot >= 0 else None, slot, st1=st1)
                 cur, nxt = nxt, cur
         if eng.T:
             for s in range(self.A - 1, -1, -1):

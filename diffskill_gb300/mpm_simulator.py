@@ -144,7 +144,7 @@ class MPMSimulator:
     def substep_grad(self, s: int) -> None:
         """``substep_grad`` (mpm_simulator.py:325-345): frame-(s+1) adjoint -> frame s (accumulated)."""
         self._eng.substep_bwd(self._frames[s], self._gframes[s + 1], self._tmp, self._pose[s], self._pose[s + 1],
-                              self._g_pose[s], self._g_pose[s + 1])
+                              self._g_pose[s], self._g_pose[s + 1], st1=self._frames[s + 1])
         self._gframes[s].add_(self._tmp)
 
     def step(self, is_copy: bool, action=None) -> None:

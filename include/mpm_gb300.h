@@ -146,10 +146,12 @@ int mpm_substep_fwd(MpmHandle* h, const void* state_f, void* state_f1, const dou
 /* Adjoint of one substep (MPMSimulator.substep_grad, mpm_simulator.py:325-345:
  * recompute grid, g2p.grad, grid_op.grad, p2g.grad, svd_grad,
  * compute_F_tmp.grad).  g_state_f1 -> g_state_f (overwritten).
+ * state_f1 (may be NULL): frame f+1 as the forward produced it; its v rows
+ * replace a second grid gather in g2p.grad.
  * g_pose_f, g_pose_f1: double[n_tools][8], accumulated. */
-int mpm_substep_bwd(MpmHandle* h, const void* state_f, const void* g_state_f1, void* g_state_f,
-                    const double* pose_f, const double* pose_f1, double* g_pose_f, double* g_pose_f1,
-                    void* stream);
+int mpm_substep_bwd(MpmHandle* h, const void* state_f, const void* state_f1, const void* g_state_f1,
+                    void* g_state_f, const double* pose_f, const double* pose_f1, double* g_pose_f,
+                    double* g_pose_f1, void* stream);
 
 /* mpm_substep_fwd that also keeps the substep's forward grid in store slot
  * `slot` (no counterpart in the reference, whose substep_grad always
@@ -158,9 +160,9 @@ int mpm_substep_fwd_store(MpmHandle* h, const void* state_f, void* state_f1, con
                           const double* pose_f1, const MpmGridStore* store, int32_t slot, void* stream);
 /* mpm_substep_bwd that restores the forward grid from store slot `slot` when
  * it was stored, and recomputes it otherwise. */
-int mpm_substep_bwd_store(MpmHandle* h, const void* state_f, const void* g_state_f1, void* g_state_f,
-                          const double* pose_f, const double* pose_f1, double* g_pose_f, double* g_pose_f1,
-                          const MpmGridStore* store, int32_t slot, void* stream);
+int mpm_substep_bwd_store(MpmHandle* h, const void* state_f, const void* state_f1, const void* g_state_f1,
+                          void* g_state_f, const double* pose_f, const double* pose_f1, double* g_pose_f,
+                          double* g_pose_f1, const MpmGridStore* store, int32_t slot, void* stream);
 
 /* compute_grid_m_kernel on a cleared grid (mpm_simulator.py:456-471).
  * grid_m: real[n_scenes][n_grid^3] written. */
