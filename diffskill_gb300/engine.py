@@ -317,10 +317,17 @@ class Horizon:
     ``ckpt_every`` = k: the state is kept every k substeps (k=1 keeps every
     frame, as the reference does); the backward pass recomputes each segment
     of k substeps from its checkpoint before running its adjoint.
+
+    ``resort_every`` = R (a multiple of k; default one action rounded up to a
+    multiple of k, 0 = never): at every R-th frame the particles of each scene
+    are re-sorted by grid cell so the scatter and gather kernels keep their
+    locality as the material deforms.  The adjoint applies the inverse
+    permutation to the frame gradient at the same frames.  Losses and action
+    gradients do not depend on the particle order.
     """
 
     def __init__(self, eng: MpmEngine, n_actions: int, ckpt_every: int = 10, store_grids: bool = True,
-                 store_budget_bytes: Optional[int] = None):
+                 store_budget_bytes: Optional[int] = None, resort_every: Optional[int] = None):
         self.eng = eng
         self.A = int(n_actions)
         self.F = self.A * eng.n_sub
@@ -355,6 +362,18 @@ class Horizon:
                 store_budget_bytes = free // 4
             worst = n_slots * eng.S * (eng.n_grid // 4) ** 3
             self.store = GridStore(eng, n_slots, min(worst, store_budget_bytes // block_bytes))
+        # periodic re-sorting of the particles by cell
+        if resort_every is None:
+            resort_every = k * (-(-eng.n_sub // k))
+        R = int(resort_every)
+        if R and R % k != 0:
+            raise ValueError(f"resort_every ({R}) must be a multiple of the checkpoint interval ({k})")
+        self.R = R if 0 < R < self.F else 0
+        self.boundaries = list(range(self.R, self.F, self.R)) if self.R else []
+        self.perms = torch.zeros((max(len(self.boundaries), 1), max(eng.P, 1)), dtype=torch.int64, device=dev)
+        counts = torch.as_tensor(np.diff(eng.offsets), device=dev)
+        self.pscene = torch.repeat_interleave(torch.arange(eng.S, device=dev), counts)
+        self._tmp = torch.empty((N_ROWS, max(eng.P, 1)), dtype=dt, device=dev)
 
     def bytes(self) -> int:
         return sum(t.numel() * t.element_size() for t in
@@ -364,6 +383,30 @@ class Horizon:
     @property
     def final(self) -> torch.Tensor:
         return self.ckpt[self.n_ckpt - 1]
+
+    def _sort_frame(self, frame: torch.Tensor, b: int) -> None:
+        """Sort the particles of ``frame`` by (scene, 4^3 block, cell) in place; keep the permutation."""
+        eng, P = self.eng, self.eng.P
+        if P == 0:
+            return
+        n = eng.n_grid
+        base = (frame[0:3, :P] * n - 0.5).to(torch.int64).clamp_(0, n - 1)
+        nb = n // 4
+        blk = ((base[0] >> 2) * nb + (base[1] >> 2)) * nb + (base[2] >> 2)
+        loc = ((base[0] & 3) << 4) | ((base[1] & 3) << 2) | (base[2] & 3)
+        key = (self.pscene * (nb ** 3) + blk) * 64 + loc
+        perm = torch.argsort(key)
+        self.perms[b].copy_(perm)
+        torch.index_select(frame[:, :P], 1, perm, out=self._tmp)
+        frame[:, :P].copy_(self._tmp)
+
+    def _unsort_grad(self, g: torch.Tensor, b: int) -> None:
+        """Adjoint of ``_sort_frame``: bring a frame gradient back to the order before boundary ``b``."""
+        P = self.eng.P
+        if P == 0:
+            return
+        self._tmp.copy_(g[:, :P])
+        g[:, :P].index_copy_(1, self.perms[b], self._tmp)
 
     def forward(self, state0: torch.Tensor, actions: torch.Tensor, pose0: Optional[torch.Tensor] = None) -> None:
         """Run all actions: ``GradModel.forward_step`` for each action (function.py:166-175)."""
@@ -384,6 +427,8 @@ class Horizon:
             else:
                 nxt = self.seg[(f + 1) % 2]
             eng.substep(cur, nxt, self.pose[f], self.pose[f + 1], store, f)
+            if self.R and (f + 1) % self.R == 0 and f + 1 < self.F:
+                self._sort_frame(nxt, (f + 1) // self.R - 1)
             cur = nxt
 
     def loss(self, targets: torch.Tensor, density_weight: float = 1.0, contact_weight: float = 0.0,
@@ -440,9 +485,14 @@ class Horizon:
                 f = c * k + i
                 slot = -1 if store is None else (f if k == 1 else i)
                 st1 = frames[i + 1] if i + 1 < k else self.ckpt[c + 1]
+                if self.R and (f + 1) % self.R == 0 and f + 1 < self.F:
+                    st1 = None  # frame f+1 was re-sorted after this substep produced it
                 eng.substep_bwd(frames[i], cur, nxt, self.pose[f], self.pose[f + 1], self.g_pose[f],
                                 self.g_pose[f + 1], store if slot >= 0 else None, slot, st1=st1)
                 cur, nxt = nxt, cur
+            f0 = c * k
+            if self.R and f0 > 0 and f0 % self.R == 0:
+                self._unsort_grad(cur, f0 // self.R - 1)
         if eng.T:
             for s in range(self.A - 1, -1, -1):
                 eng.tools_action_bwd(self.vel[s * n], self.pose[s * n], self.g_pose[s * n], self.g_act[s])

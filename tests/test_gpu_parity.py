@@ -313,3 +313,27 @@ def test_grid_store_restore_equals_recompute(gpu_lib, k):
     for l, g in out[1:]:
         assert abs(l - l0) <= 1e-12 * abs(l0)
         assert rel_err(g, g0) < 1e-9
+
+
+@pytest.mark.parametrize("k", [1, 10])
+def test_resorting_particles_keeps_loss_and_gradients(gpu_lib, k):
+    """Re-sorting particles by cell at every action boundary (and unsorting the
+    frame gradient in the adjoint) leaves the loss and action gradients as they are."""
+    sc = small_scene(n=5000, n_actions=3, substeps=20, tools=[all_tools()[0], all_tools()[2]], precision="fp64")
+    eng = make_engine(sc)
+    res = []
+    for R in (0, 20):
+        hz = Horizon(eng, sc.n_actions, ckpt_every=k, resort_every=R)
+        assert hz.R == R
+        hz.forward(eng.init_state([sc.x0]), eng.expand_actions([sc.actions]))
+        loss = float(hz.loss(eng.targets([sc.target])).sum())
+        g = eng.collapse_action_grad(hz.backward())[0].cpu().numpy()
+        torch.cuda.synchronize()
+        res.append((loss, g, hz.g_state0[:, :sc.n_particles].clone()))
+        if R:
+            assert not torch.equal(hz.perms[0][:sc.n_particles].cpu(), torch.arange(sc.n_particles))
+    (l0, g0, s0), (l1, g1, s1) = res
+    assert abs(l1 - l0) <= 1e-12 * abs(l0)
+    assert rel_err(g1, g0) < 1e-9
+    # the gradient w.r.t. the initial state comes back in the original particle order
+    assert rel_err(s1.cpu().numpy(), s0.cpu().numpy()) < 1e-9
