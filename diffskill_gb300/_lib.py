@@ -66,6 +66,11 @@ SIGNATURES = {
     "mpm_density_l1": (_i32, [_c_p, _c_p, _c_p, _f64, _c_p, _c_p, _c_p]),
     "mpm_soft_contact": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_soft_contact_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
+    "mpm_target_sdf": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _i32, _c_p]),
+    "mpm_sdf_loss": (_i32, [_c_p, _c_p, _c_p, _f64, _c_p, _c_p, _c_p]),
+    "mpm_iou": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p]),
+    "mpm_contact_min_dist": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
+    "mpm_contact_min_dist_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_tool_distance_cols": (_i32, [_c_p]),
     "mpm_tool_distance": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_tool_distance_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),

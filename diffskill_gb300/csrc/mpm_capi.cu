@@ -25,6 +25,7 @@ struct MpmHandle {
   int n_tools = 0;
   std::vector<MpmToolDesc> h_tools;
   unsigned int* d_status = nullptr;
+  int* d_flags = nullptr;  // convergence flags of mpm_target_sdf
   void* grid[4] = {nullptr, nullptr, nullptr, nullptr};
   unsigned char* d_blockbuf = nullptr;
   int* d_active = nullptr;
@@ -125,14 +126,13 @@ int check_aligned(MpmHandle* h, const void* ptr, const char* name, bool allow_nu
 // ---------------------------------------------------------------------------
 // tool kinematics (FP64): set_velocity + forward_kinematics per action
 // ---------------------------------------------------------------------------
-__device__ void fk_step(const MpmToolDesc& d, const double* p0, const double* vv, double* p1) {
+// wq = w2quat(vv[3..5]), computed once per action by the caller
+__device__ void fk_step(const MpmToolDesc& d, const double* p0, const double* vv, const double* wq, double* p1) {
   for (int k = 0; k < 3; ++k) {
     double a = p0[k] + vv[k];
     double mn = (a < d.upper[k]) ? a : d.upper[k];
     p1[k] = (d.lower[k] < mn) ? mn : d.lower[k];
   }
-  double wq[4];
-  mpm::w2quat(vv + 3, wq);
   if (d.type == mpm::TOOL_GRIPPER) {
     mpm::qmul(p0 + 3, wq, p1 + 3);  // Gripper: rotation[f] * w2quat(w) (primitives.py:460)
     double a = p0[7] - vv[6];
@@ -156,11 +156,12 @@ __global__ void k_tools_action(const MpmToolDesc* __restrict__ tools, int n_tool
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_tools) return;
   const MpmToolDesc d = tools[t];
-  double vv[8];
+  double vv[8], wq[4];
   action_velocity(d, action + 8 * t, n_sub, vv);
+  mpm::w2quat(vv + 3, wq);  // the same for every substep of the action
   for (int j = 0; j < n_sub; ++j) {
     for (int k = 0; k < 8; ++k) vel[((int64_t)j * n_tools + t) * 8 + k] = vv[k];
-    fk_step(d, pose + ((int64_t)j * n_tools + t) * 8, vv, pose + ((int64_t)(j + 1) * n_tools + t) * 8);
+    fk_step(d, pose + ((int64_t)j * n_tools + t) * 8, vv, wq, pose + ((int64_t)(j + 1) * n_tools + t) * 8);
   }
 }
 __global__ void k_tools_action_bwd(const MpmToolDesc* __restrict__ tools, int n_tools, const double* __restrict__ vel,
@@ -170,11 +171,23 @@ __global__ void k_tools_action_bwd(const MpmToolDesc* __restrict__ tools, int n_
   if (t >= n_tools) return;
   const MpmToolDesc d = tools[t];
   double gvv_sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  // w2quat and its adjoint are evaluated once per run of substeps with the
+  // same angular velocity (set_velocity writes one per action): the
+  // quaternion gradient is summed over the run first (w2quat_vjp is linear in it)
+  double w_run[3] = {0, 0, 0}, wq[4] = {1, 0, 0, 0}, gwq_run[4] = {0, 0, 0, 0};
+  bool have_run = false;
   for (int j = n_sub - 1; j >= 0; --j) {
     const double* p0 = pose + ((int64_t)j * n_tools + t) * 8;
     const double* vv = vel + ((int64_t)j * n_tools + t) * 8;
     const double* g1 = g_pose + ((int64_t)(j + 1) * n_tools + t) * 8;
     double* g0 = g_pose + ((int64_t)j * n_tools + t) * 8;
+    if (!have_run || vv[3] != w_run[0] || vv[4] != w_run[1] || vv[5] != w_run[2]) {
+      if (have_run) mpm::w2quat_vjp(w_run, gwq_run, gvv_sum + 3);
+      for (int k = 0; k < 3; ++k) w_run[k] = vv[3 + k];
+      for (int k = 0; k < 4; ++k) gwq_run[k] = 0.0;
+      mpm::w2quat(w_run, wq);
+      have_run = true;
+    }
     double gvv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int k = 0; k < 3; ++k) {
       double a = p0[k] + vv[k];
@@ -184,8 +197,7 @@ __global__ void k_tools_action_bwd(const MpmToolDesc* __restrict__ tools, int n_
         gvv[k] += g1[k];
       }
     }
-    double wq[4], gwq[4] = {0, 0, 0, 0};
-    mpm::w2quat(vv + 3, wq);
+    double gwq[4] = {0, 0, 0, 0};
     if (d.type == mpm::TOOL_GRIPPER) {
       mpm::qmul_vjp(p0 + 3, wq, g1 + 3, g0 + 3, gwq);
       double a = p0[7] - vv[6];
@@ -198,9 +210,10 @@ __global__ void k_tools_action_bwd(const MpmToolDesc* __restrict__ tools, int n_
       mpm::qmul_vjp(wq, p0 + 3, g1 + 3, gwq, g0 + 3);
       g0[7] += g1[7];
     }
-    mpm::w2quat_vjp(vv + 3, gwq, gvv + 3);
+    for (int k = 0; k < 4; ++k) gwq_run[k] += gwq[k];
     for (int k = 0; k < 8; ++k) gvv_sum[k] += gvv[k];
   }
+  if (have_run) mpm::w2quat_vjp(w_run, gwq_run, gvv_sum + 3);
   // set_velocity.grad: v = a * scale / n_sub for every substep of the action
   if (d.action_dim > 0) {
     for (int k = 0; k < 3; ++k) g_action[8 * t + k] += gvv_sum[k] * d.action_scale[k] / n_sub;
@@ -257,6 +270,7 @@ int mpm_create(const MpmParams* params, const int64_t* scene_offsets, MpmHandle*
   ok = ok && cudaMalloc(&h->d_pscene, std::max<size_t>(1, ps.size()) * sizeof(int)) == cudaSuccess;
   ok = ok && cudaMalloc(&h->d_tool_off, toff.size() * sizeof(int)) == cudaSuccess;
   ok = ok && cudaMalloc(&h->d_status, sizeof(unsigned int)) == cudaSuccess;
+  ok = ok && cudaMalloc(&h->d_flags, 4 * sizeof(int)) == cudaSuccess;
   for (int i = 0; i < 4 && ok; ++i) ok = cudaMalloc(&h->grid[i], gbytes) == cudaSuccess;
   const int64_t nb = p.n_grid / 4;
   const int64_t nblocks = (int64_t)p.n_scenes * nb * nb * nb;
@@ -288,6 +302,7 @@ int mpm_destroy(MpmHandle* h) {
   cudaFree(h->d_col_off);
   cudaFree(h->d_tools);
   cudaFree(h->d_status);
+  cudaFree(h->d_flags);
   for (int i = 0; i < 4; ++i) cudaFree(h->grid[i]);
   cudaFree(h->d_blockbuf);
   cudaFree(h->d_active);
@@ -554,6 +569,91 @@ int mpm_soft_contact_bwd(MpmHandle* h, const void* state, const double* pose, co
                       : mpm::launch_soft_contact_bwd<float>(L, h->n_tools, (const float*)state, pose, sums,
                                                             g_min_dist, (float*)g_state, g_pose);
   return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_soft_contact_bwd");
+}
+
+int mpm_target_sdf(MpmHandle* h, const void* target_density, void* target_sdf, void* nearest, void* work,
+                   int32_t n_iters, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_target_sdf: NULL handle");
+  if (n_iters < 0) return fail(h, MPM_E_INVALID, "mpm_target_sdf: n_iters < 0");
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, target_density, "target_density"));
+  MPM_TRY(check_aligned(h, target_sdf, "target_sdf"));
+  MPM_TRY(check_aligned(h, nearest, "nearest"));
+  MPM_TRY(check_aligned(h, work, "work"));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e = h->p.precision == MPM_PREC_FP64
+                      ? mpm::launch_target_sdf<double>(L, h->d_flags, (const double*)target_density,
+                                                       (double*)target_sdf, (double*)nearest, (double*)work, n_iters)
+                      : mpm::launch_target_sdf<float>(L, h->d_flags, (const float*)target_density,
+                                                      (float*)target_sdf, (float*)nearest, (float*)work, n_iters);
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_target_sdf");
+}
+
+int mpm_sdf_loss(MpmHandle* h, const void* grid_m, const void* target_sdf, double weight, double* loss,
+                 void* g_grid_m, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_sdf_loss: NULL handle");
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, grid_m, "grid_m"));
+  MPM_TRY(check_aligned(h, target_sdf, "target_sdf"));
+  MPM_TRY(check_aligned(h, loss, "loss"));
+  MPM_TRY(check_aligned(h, g_grid_m, "g_grid_m", true));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e = h->p.precision == MPM_PREC_FP64
+                      ? mpm::launch_sdf_loss<double>(L, (const double*)grid_m, (const double*)target_sdf, weight,
+                                                     loss, (double*)g_grid_m)
+                      : mpm::launch_sdf_loss<float>(L, (const float*)grid_m, (const float*)target_sdf, weight, loss,
+                                                    (float*)g_grid_m);
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_sdf_loss");
+}
+
+int mpm_iou(MpmHandle* h, const void* grid_m, const void* target, double* iou, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_iou: NULL handle");
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, grid_m, "grid_m"));
+  MPM_TRY(check_aligned(h, target, "target"));
+  MPM_TRY(check_aligned(h, iou, "iou"));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e = h->p.precision == MPM_PREC_FP64
+                      ? mpm::launch_iou<double>(L, (const double*)grid_m, (const double*)target, iou)
+                      : mpm::launch_iou<float>(L, (const float*)grid_m, (const float*)target, iou);
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_iou");
+}
+
+int mpm_contact_min_dist(MpmHandle* h, const void* state, const double* pose, double* min_dist, int64_t* argmin,
+                         void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_contact_min_dist: NULL handle");
+  if (h->n_tools == 0) return MPM_OK;
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, state, "state"));
+  MPM_TRY(check_aligned(h, pose, "pose"));
+  MPM_TRY(check_aligned(h, min_dist, "min_dist"));
+  MPM_TRY(check_aligned(h, argmin, "argmin"));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e =
+      h->p.precision == MPM_PREC_FP64
+          ? mpm::launch_contact_min<double>(L, h->n_tools, (const double*)state, pose, min_dist, argmin)
+          : mpm::launch_contact_min<float>(L, h->n_tools, (const float*)state, pose, min_dist, argmin);
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_contact_min_dist");
+}
+
+int mpm_contact_min_dist_bwd(MpmHandle* h, const void* state, const double* pose, const int64_t* argmin,
+                             const double* g_min_dist, void* g_state, double* g_pose, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_contact_min_dist_bwd: NULL handle");
+  if (h->n_tools == 0) return MPM_OK;
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, state, "state"));
+  MPM_TRY(check_aligned(h, pose, "pose"));
+  MPM_TRY(check_aligned(h, argmin, "argmin"));
+  MPM_TRY(check_aligned(h, g_min_dist, "g_min_dist"));
+  MPM_TRY(check_aligned(h, g_state, "g_state"));
+  MPM_TRY(check_aligned(h, g_pose, "g_pose"));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e = h->p.precision == MPM_PREC_FP64
+                      ? mpm::launch_contact_min_bwd<double>(L, h->n_tools, (const double*)state, pose, argmin,
+                                                            g_min_dist, (double*)g_state, g_pose)
+                      : mpm::launch_contact_min_bwd<float>(L, h->n_tools, (const float*)state, pose, argmin,
+                                                           g_min_dist, (float*)g_state, g_pose);
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_contact_min_dist_bwd");
 }
 
 int mpm_tool_distance_cols(MpmHandle* h) { return h ? h->n_cols : 0; }

@@ -1,5 +1,5 @@
 // Internal launch interface between the C ABI (mpm_capi.cu) and the kernel
-// translation units (mpm_fwd.cu, mpm_bwd.cu).
+// translation units (mpm_fwd.cu, mpm_bwd.cu, mpm_loss.cu).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -92,6 +92,18 @@ cudaError_t launch_tool_distance(const LaunchCtx& L, const int* col_off, int n_c
 template <typename T>
 cudaError_t launch_tool_distance_bwd(const LaunchCtx& L, const int* col_off, const T* st, const double* pose,
                                      const T* g_out, T* gst, double* g_pose);
+template <typename T>
+cudaError_t launch_target_sdf(const LaunchCtx& L, int* flags, const T* dens, T* sdf, T* near, T* work, int n_iters);
+template <typename T>
+cudaError_t launch_sdf_loss(const LaunchCtx& L, const T* gm, const T* sdf, double weight, double* loss, T* ggm);
+template <typename T>
+cudaError_t launch_iou(const LaunchCtx& L, const T* gm, const T* tgt, double* iou);
+template <typename T>
+cudaError_t launch_contact_min(const LaunchCtx& L, int n_tools, const T* st, const double* pose, double* min_dist,
+                               int64_t* argmin);
+template <typename T>
+cudaError_t launch_contact_min_bwd(const LaunchCtx& L, int n_tools, const T* st, const double* pose,
+                                   const int64_t* argmin, const double* g_min, T* gst, double* g_pose);
 template <typename T>
 cudaError_t launch_soft_contact_bwd(const LaunchCtx& L, int n_tools, const T* st, const double* pose,
                                     const double* sums, const double* g_min, T* gst, double* g_pose);

@@ -220,6 +220,47 @@ class MpmEngine:
         _lib.check(self.lib.mpm_soft_contact_bwd(self.h, _ptr(st), _ptr(pose), _ptr(sums), _ptr(g_md), _ptr(g_st),
                                                  _ptr(g_pose), _stream()), self.h, "mpm_soft_contact_bwd")
 
+    def target_sdf(self, density: torch.Tensor, n_iters: Optional[int] = None) -> tuple:
+        """``Loss.update_target`` (loss.py:129-134) on [S, G] target densities:
+        returns (target_sdf [S, G], nearest [S, G, 3]); ``n_iters`` defaults to
+        the reference's 2 * n_grid."""
+        n_iters = 2 * self.n_grid if n_iters is None else int(n_iters)
+        density = density.to(self.device, self.dtype).contiguous()
+        # (with n_iters = 0 they stay as a fresh taichi field starts: zero)
+        sdf = torch.zeros((self.S, self.G), dtype=self.dtype, device=self.device)
+        near = torch.zeros((self.S, self.G, 3), dtype=self.dtype, device=self.device)
+        work = torch.empty((self.S, self.G, 4), dtype=self.dtype, device=self.device)
+        _lib.check(self.lib.mpm_target_sdf(self.h, _ptr(density), _ptr(sdf), _ptr(near), _ptr(work), n_iters,
+                                           _stream()), self.h, "mpm_target_sdf")
+        return sdf, near
+
+    def sdf_loss(self, gm, target_sdf, weight: float = 1.0, g_gm=None) -> torch.Tensor:
+        """[S] weight * sum target_sdf * grid_m; adds weight * target_sdf to ``g_gm``."""
+        loss = torch.empty(self.S, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.mpm_sdf_loss(self.h, _ptr(gm), _ptr(target_sdf), float(weight), _ptr(loss), _ptr(g_gm),
+                                         _stream()), self.h, "mpm_sdf_loss")
+        return loss
+
+    def iou(self, gm, target) -> torch.Tensor:
+        """[S] ``iou_kernel`` (loss.py:294-308) of each scene's grid mass and target."""
+        out = torch.empty(self.S, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.mpm_iou(self.h, _ptr(gm), _ptr(target), _ptr(out), _stream()), self.h, "mpm_iou")
+        return out
+
+    def contact_min_dist(self, st, pose) -> tuple:
+        """Hard contact distance of every tool: (min_dist [T] double, argmin [T] int64)."""
+        md = torch.empty(max(self.T, 1), dtype=torch.float64, device=self.device)
+        am = torch.full((max(self.T, 1),), -1, dtype=torch.int64, device=self.device)
+        _lib.check(self.lib.mpm_contact_min_dist(self.h, _ptr(st), _ptr(pose), _ptr(md), _ptr(am), _stream()),
+                   self.h, "mpm_contact_min_dist")
+        return md[:self.T], am
+
+    def contact_min_dist_bwd(self, st, pose, argmin, g_md, g_st, g_pose) -> None:
+        g_md = g_md.to(self.device, torch.float64).contiguous()
+        _lib.check(self.lib.mpm_contact_min_dist_bwd(self.h, _ptr(st), _ptr(pose), _ptr(argmin), _ptr(g_md),
+                                                     _ptr(g_st), _ptr(g_pose), _stream()), self.h,
+                   "mpm_contact_min_dist_bwd")
+
     @property
     def n_dist_cols(self) -> int:
         return int(self.lib.mpm_tool_distance_cols(self.h))

@@ -190,6 +190,48 @@ int mpm_soft_contact(MpmHandle* h, const void* state, const double* pose, double
 int mpm_soft_contact_bwd(MpmHandle* h, const void* state, const double* pose, const double* sums,
                          const double* g_min_dist, void* g_state, double* g_pose, void* stream);
 
+/* update_target (loss.py:129-134): update_target_sdf (loss.py:105-124)
+ * iterated n_iters times from a copy filled with inf = 1000 (the reference
+ * runs 2*n_grid iterations).  A node with target density > 1e-4 gets sdf 0
+ * and itself as nearest point; any other node the first strict minimum over
+ * the offsets (-3..2)^3 \ {0}, in the reference's loop order, of
+ * sqrt(|I*dx - nearest_copy[v]|^2 + 1e-8) over neighbours with sdf_copy < inf,
+ * else inf.  target_density: real[n_scenes][n_grid^3]; target_sdf:
+ * real[n_scenes][n_grid^3] and nearest: real[n_scenes][n_grid^3][3] written
+ * (nearest = 0 where sdf stays inf); work: real[n_scenes][n_grid^3][4]
+ * scratch.  Launches after the first iteration that changes no node return
+ * at once (every later iteration would reproduce it). */
+int mpm_target_sdf(MpmHandle* h, const void* target_density, void* target_sdf, void* nearest, void* work,
+                   int32_t n_iters, void* stream);
+
+/* compute_sdf_loss_kernel (loss.py:178-180) per scene, FP64 sum in a fixed
+ * order: loss[s] = weight * sum_I target_sdf * grid_m (double[n_scenes],
+ * overwritten).  If g_grid_m is not NULL, weight * target_sdf is ADDED to it,
+ * so it can follow mpm_density_l1 (which overwrites). */
+int mpm_sdf_loss(MpmHandle* h, const void* grid_m, const void* target_sdf, double weight, double* loss,
+                 void* g_grid_m, void* stream);
+
+/* iou_kernel (loss.py:294-308) per scene in FP64: ma = max(0, max m),
+ * mb = max(0, max t), I = sum m t / ma / mb, U = sum m / ma + sum t / mb,
+ * iou[s] = I / (U - I) (double[n_scenes]).  No adjoint: the reference's
+ * iou_grad is empty (loss.py:318-321). */
+int mpm_iou(MpmHandle* h, const void* grid_m, const void* target, double* iou, void* stream);
+
+/* Hard contact distance (compute_contact_distance_kernel, loss.py:151-155,
+ * started from 100000 as compute_loss_kernel does, loss.py:243-244):
+ * min_dist[t] = min(100000, min_i max(sdf_t(x_i), 0)) over the particles of
+ * tool t's scene (double[n_tools]); argmin[t] = the lowest particle index
+ * attaining it, or -1 (int64[n_tools]).  Tools with action_dim 0 get 0 and -1
+ * (Loss keeps movable tools only, loss.py:21-25). */
+int mpm_contact_min_dist(MpmHandle* h, const void* state, const double* pose, double* min_dist, int64_t* argmin,
+                         void* stream);
+/* Adjoint: g_min_dist[t] flows to the particle argmin[t] (x rows of g_state,
+ * accumulated) and to the tool pose (g_pose, double[n_tools][8],
+ * accumulated) through max(sdf, 0), which passes it only where sdf > 0.
+ * Ties send the whole gradient to the lowest index. */
+int mpm_contact_min_dist_bwd(MpmHandle* h, const void* state, const double* pose, const int64_t* argmin,
+                             const double* g_min_dist, void* g_state, double* g_pose, void* stream);
+
 /* Per-particle tool distances (GradModel.compute_min_dist, function.py:79-89):
  * column c of out (real[n_cols][ld], n_cols from mpm_tool_distance_cols) holds
  * the SDF of the tool owning column c at every particle of that tool's scene

@@ -1667,4 +1667,93 @@ double oracle_soft_contact(const OracleTool* tool, const double* pose, int64_t n
   return md;
 }
 
+// update_target (loss.py:129-134): the copy is filled with inf = 1000, then
+// update_target_sdf (loss.py:105-124) runs n_iters times.  Every node reads
+// only the previous iteration's copy; offsets are visited in the order of
+// ti.ndrange((-3,3),(-3,3),(-3,3)) and the first strict minimum of
+// norm(grid_pos - nearest) = sqrt(|d|^2 + 1e-8) wins.  T is the simulator's
+// float type; each operation is rounded to T (built with -ffp-contract=off).
+// Nodes whose sdf stays inf get nearest = 0.
+}  // extern "C"
+template <typename T>
+static void target_sdf_impl(int n, double dx, int n_iters, const T* dens, T* sdf, T* nearest) {
+  const int64_t G = (int64_t)n * n * n;
+  const T inf = T(1000.0);
+  std::vector<T> sc(G, inf), nc(3 * G, T(0));
+  for (int64_t i = 0; i < G; ++i) {
+    sdf[i] = inf;
+    nearest[3 * i] = nearest[3 * i + 1] = nearest[3 * i + 2] = T(0);
+  }
+  for (int it = 0; it < n_iters; ++it) {
+#pragma omp parallel for schedule(static)
+    for (int64_t id = 0; id < G; ++id) {
+      const int i0 = (int)(id / ((int64_t)n * n)), i1 = (int)((id / n) % n), i2 = (int)(id % n);
+      const T gp[3] = {T(double(i0) * dx), T(double(i1) * dx), T(double(i2) * dx)};
+      T best = inf, bn[3] = {T(0), T(0), T(0)};
+      if (double(dens[id]) > 1e-4) {
+        best = T(0);
+        bn[0] = gp[0];
+        bn[1] = gp[1];
+        bn[2] = gp[2];
+      } else {
+        for (int a = -3; a < 3; ++a)
+          for (int b = -3; b < 3; ++b)
+            for (int c = -3; c < 3; ++c) {
+              const int v0 = i0 + a, v1 = i1 + b, v2 = i2 + c;
+              if (std::min(v0, std::min(v1, v2)) < 0 || std::max(v0, std::max(v1, v2)) >= n) continue;
+              if (std::abs(a) + std::abs(b) + std::abs(c) == 0) continue;
+              const int64_t v = ((int64_t)v0 * n + v1) * n + v2;
+              if (!(sc[v] < inf)) continue;
+              const T d0 = gp[0] - nc[3 * v], d1 = gp[1] - nc[3 * v + 1], d2 = gp[2] - nc[3 * v + 2];
+              const T dist = std::sqrt(T(T(T(d0 * d0) + T(d1 * d1)) + T(d2 * d2)) + T(1e-8));
+              if (dist < best) {
+                best = dist;
+                bn[0] = nc[3 * v];
+                bn[1] = nc[3 * v + 1];
+                bn[2] = nc[3 * v + 2];
+              }
+            }
+      }
+      sdf[id] = best;
+      nearest[3 * id] = bn[0];
+      nearest[3 * id + 1] = bn[1];
+      nearest[3 * id + 2] = bn[2];
+    }
+    std::copy(sdf, sdf + G, sc.begin());
+    std::copy(nearest, nearest + 3 * G, nc.begin());
+  }
+}
+extern "C" {
+void oracle_target_sdf_f64(int n, double dx, int n_iters, const double* dens, double* sdf, double* nearest) {
+  target_sdf_impl<double>(n, dx, n_iters, dens, sdf, nearest);
+}
+void oracle_target_sdf_f32(int n, double dx, int n_iters, const float* dens, float* sdf, float* nearest) {
+  target_sdf_impl<float>(n, dx, n_iters, dens, sdf, nearest);
+}
+
+// hard contact distance (compute_contact_distance_kernel, loss.py:151-155)
+// of one movable tool, started from 100000 (loss.py:243-244):
+// min(100000, min_i max(sdf(x_i), 0)); *argmin = lowest index attaining it or
+// -1.  With g_min != 0 the gradient goes to that particle (x part of g_state)
+// and to g_pose, where sdf > 0.
+double oracle_contact_min(const OracleTool* tool, const double* pose, int64_t n, const double* state, double g_min,
+                          double* g_state, double* g_pose, int64_t* argmin) {
+  double md = 100000.0;
+  int64_t am = -1;
+  for (int64_t i = 0; i < n; ++i) {
+    const double sd = tool_sdf(*tool, pose, state + 24 * i);
+    const double d = (0.0 < sd) ? sd : 0.0;
+    if (d < md) {
+      md = d;
+      am = i;
+    } else if (d == md && am < 0) {
+      am = i;
+    }
+  }
+  if (argmin) *argmin = am;
+  if (g_min != 0 && g_state && am >= 0 && 0.0 < tool_sdf(*tool, pose, state + 24 * am))
+    tool_sdf_vjp(*tool, pose, state + 24 * am, g_min, g_state + 24 * am, g_pose);
+  return md;
+}
+
 }  // extern "C"

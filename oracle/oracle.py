@@ -56,7 +56,8 @@ def build(force: bool = False, quiet: bool = True) -> str:
     """Compile the oracle with g++ (OpenMP).  Returns the library path."""
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
         return LIB
-    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-o", LIB + ".tmp", SRC]
+    # -ffp-contract=off: every operation rounded on its own, on x86 and Arm alike
+    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-o", LIB + ".tmp", SRC]
     subprocess.run(cmd, check=True, capture_output=quiet)
     os.replace(LIB + ".tmp", LIB)
     return LIB
@@ -78,6 +79,12 @@ def lib():
         L.oracle_soft_contact.restype = ctypes.c_double
         L.oracle_num_threads.restype = ctypes.c_int
         L.oracle_soft_contact.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int64, _dp, ctypes.c_double, _dp, _dp]
+        L.oracle_contact_min.restype = ctypes.c_double
+        L.oracle_contact_min.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int64, _dp, ctypes.c_double, _dp, _dp,
+                                         ctypes.POINTER(ctypes.c_int64)]
+        L.oracle_target_sdf_f64.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp, _dp, _dp]
+        _fp = ctypes.POINTER(ctypes.c_float)
+        L.oracle_target_sdf_f32.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, _fp, _fp, _fp]
         _lib = L
     return _lib
 
@@ -132,6 +139,40 @@ def init_state(x0: np.ndarray) -> np.ndarray:
     st[:, 0:3] = x0
     st[:, 15] = st[:, 19] = st[:, 23] = 1.0
     return st
+
+
+def target_sdf(density: np.ndarray, dx: float, n_iters: int, single: bool = False):
+    """``update_target`` (loss.py:129-134, update_target_sdf 105-124) on one
+    (n,n,n) target density; ``single`` rounds every operation to FP32 as the
+    FP32 simulator does.  Returns (sdf (n,n,n), nearest (n,n,n,3))."""
+    n = density.shape[0]
+    dt = np.float32 if single else np.float64
+    d = np.ascontiguousarray(density, dtype=dt)
+    sdf = np.empty((n, n, n), dtype=dt)
+    near = np.empty((n, n, n, 3), dtype=dt)
+    if single:
+        fp = ctypes.POINTER(ctypes.c_float)
+        lib().oracle_target_sdf_f32(n, float(dx), int(n_iters), d.ctypes.data_as(fp), sdf.ctypes.data_as(fp),
+                                    near.ctypes.data_as(fp))
+    else:
+        lib().oracle_target_sdf_f64(n, float(dx), int(n_iters), ptr(d), ptr(sdf), ptr(near))
+    return sdf, near
+
+
+def sdf_loss(grid_m: np.ndarray, target_sdf: np.ndarray):
+    """``compute_sdf_loss_kernel`` (loss.py:178-180): sum target_sdf * grid_m,
+    and its gradient w.r.t. grid_m (= target_sdf)."""
+    return float(np.sum(np.asarray(target_sdf, np.float64) * np.asarray(grid_m, np.float64))), np.array(target_sdf)
+
+
+def iou(grid_m: np.ndarray, target: np.ndarray) -> float:
+    """``iou_kernel`` (loss.py:294-308): the maxima start at 0."""
+    a = np.asarray(grid_m, np.float64).ravel()
+    b = np.asarray(target, np.float64).ravel()
+    ma, mb = max(0.0, float(a.max())), max(0.0, float(b.max()))
+    inter = float(np.sum(a * b)) / ma / mb
+    union = float(a.sum()) / ma + float(b.sum()) / mb
+    return inter / (union - inter)
 
 
 class Oracle:
@@ -203,6 +244,13 @@ class Oracle:
     def soft_contact(self, t: int, pose, state, g_min: float = 0.0, g_state=None, g_pose=None) -> float:
         return lib().oracle_soft_contact(ctypes.byref(self.tools[t]), ptr(np.ascontiguousarray(pose)),
                                          state.shape[0], ptr(state), g_min, ptr(g_state), ptr(g_pose))
+
+    def contact_min(self, t: int, pose, state, g_min: float = 0.0, g_state=None, g_pose=None):
+        """Hard contact distance of tool t and its argmin particle (loss.py:151-155)."""
+        am = ctypes.c_int64(-1)
+        md = lib().oracle_contact_min(ctypes.byref(self.tools[t]), ptr(np.ascontiguousarray(pose)), state.shape[0],
+                                      ptr(state), g_min, ptr(g_state), ptr(g_pose), ctypes.byref(am))
+        return md, int(am.value)
 
     # -- trajectory ----------------------------------------------------------
     def rollout(self, x0: np.ndarray, actions: np.ndarray, keep_frames: bool = True):

@@ -286,3 +286,109 @@ def test_baseline_config1_time_step_diverges():
     sc = scenes.config1(n_actions=4, n_particles=2000, dt=1e-4, substeps=50)
     fin = O.Oracle(sc.sim, sc.tools).rollout(sc.x0, sc.actions, keep_frames=False)["final"]
     assert np.isfinite(fin).all()
+
+
+# ---------------------------------------------------------------- loss.py terms
+def _target_sdf_python(dens, dx, n_iters):
+    """update_target (loss.py:105-134) as plain Python loops, for small grids."""
+    n = dens.shape[0]
+    inf = 1000.0
+    sc = np.full((n, n, n), inf)
+    nc = np.zeros((n, n, n, 3))
+    sdf, near = sc.copy(), nc.copy()
+    offs = [(a, b, c) for a in range(-3, 3) for b in range(-3, 3) for c in range(-3, 3)]
+    for _ in range(n_iters):
+        for i in range(n):
+            for j in range(n):
+                for k in range(n):
+                    gp = np.array([i * dx, j * dx, k * dx])
+                    sdf[i, j, k] = inf
+                    if dens[i, j, k] > 1e-4:
+                        sdf[i, j, k] = 0.0
+                        near[i, j, k] = gp
+                        continue
+                    near[i, j, k] = 0.0
+                    for a, b, c in offs:
+                        v = (i + a, j + b, k + c)
+                        if min(v) < 0 or max(v) >= n or abs(a) + abs(b) + abs(c) == 0:
+                            continue
+                        if sc[v] < inf:
+                            d = gp - nc[v]
+                            dist = np.sqrt(((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]) + 1e-8)
+                            if dist < sdf[i, j, k]:
+                                sdf[i, j, k] = dist
+                                near[i, j, k] = nc[v]
+        sc, nc = sdf.copy(), near.copy()
+    return sdf, near
+
+
+def _sparse_target(n, seed):
+    rng = np.random.default_rng(seed)
+    d = np.zeros((n, n, n))
+    d[rng.random((n, n, n)) < 0.03] = 1e-3
+    d[rng.random((n, n, n)) < 0.05] = 5e-5  # below the threshold
+    return d
+
+
+@pytest.mark.parametrize("n_iters", [1, 2, 6])
+def test_target_sdf_matches_python_restatement(n_iters):
+    d = _sparse_target(8, 3)
+    s_ref, n_ref = _target_sdf_python(d, 1 / 8, n_iters)
+    s, near = O.target_sdf(d, 1 / 8, n_iters)
+    assert np.array_equal(s, s_ref) and np.array_equal(near, n_ref)
+
+
+def test_target_sdf_converged_field_properties():
+    """After 2 n sweeps every node holds the distance to a dense node (its
+    'nearest point'), never less than the true distance to the dense set, and
+    dense nodes hold 0."""
+    n, dx = 16, 1 / 16
+    d = _sparse_target(n, 5)
+    d[d < 1e-4] = 0.0
+    s, near = O.target_sdf(d, dx, 2 * n)
+    dense = np.argwhere(d > 1e-4)
+    gp = np.stack(np.meshgrid(*[np.arange(n) * dx] * 3, indexing="ij"), -1)
+    assert (s[d > 1e-4] == 0).all()
+    assert np.allclose(s, np.sqrt(((gp - near) ** 2).sum(-1) + 1e-8) * (d <= 1e-4), atol=1e-15)
+    true = np.sqrt(((gp[:, :, :, None, :] - dense[None, None, None] * dx) ** 2).sum(-1).min(-1))
+    assert (s[d <= 1e-4] >= true[d <= 1e-4] - 1e-12).all()
+    assert (s < 1000).all()
+    # FP32 rounding of the same sweeps stays within FP32 resolution
+    s32, _ = O.target_sdf(d, dx, 2 * n, single=True)
+    assert np.abs(s32 - s).max() < 1e-6
+
+
+def test_iou_and_sdf_loss_definitions():
+    rng = np.random.default_rng(0)
+    a, b = rng.random(512), rng.random(512)
+    ma, mb = a.max(), b.max()
+    inter = (a * b).sum() / ma / mb
+    assert abs(O.iou(a, b) - inter / (a.sum() / ma + b.sum() / mb - inter)) < 1e-15
+    # identical normalised grids: I / (2 sum t / mb - I)
+    assert O.iou(a, a) == pytest.approx(((a * a).sum() / ma ** 2) / (2 * a.sum() / ma - (a * a).sum() / ma ** 2))
+    loss, g = O.sdf_loss(a, b)
+    assert loss == pytest.approx(float((a * b).sum())) and np.array_equal(g, b)
+
+
+def test_contact_min_and_its_adjoint():
+    """Hard contact distance: the minimum over particles of max(sdf, 0) and a
+    gradient through the argmin particle that matches central differences."""
+    tools = all_tools()
+    sc = small_scene(n=400, tools=tools)
+    o = O.Oracle(sc.sim, tools)
+    st = perturbed_state(sc.x0, seed=5)
+    pose = o.pose0()
+    for t in range(o.T):
+        md, am = o.contact_min(t, pose[t], st)
+        sd = np.array([o.contact_min(t, pose[t], st[i:i + 1])[0] for i in range(0, st.shape[0], 37)])
+        assert md <= sd.min() + 1e-15
+        if md <= 0:
+            continue
+        g = np.zeros_like(st)
+        gp = np.zeros(8)
+        o.contact_min(t, pose[t], st, 1.0, g, gp)
+        for d in range(3):
+            e = np.zeros_like(st)
+            e[am, d] = 1e-7
+            fd = (o.contact_min(t, pose[t], st + e)[0] - o.contact_min(t, pose[t], st - e)[0]) / 2e-7
+            assert abs(fd - g[am, d]) < 1e-5
