@@ -190,4 +190,5 @@ def test_loss_class_matches_oracle(gpu_lib, soft):
     info = L.compute_loss(0)
     assert abs(L._start_loss - ref) <= 1e-10 * abs(ref)
     assert abs(info["loss"] - 2 * ref) <= 1e-10 * abs(ref) and abs(info["reward"] + ref) <= 1e-10 * abs(ref)
-    assert info["incremental_iou"] == 0.0
+    # the same frame twice: the IoU moves only by the atomic summation order of the grid mass
+    assert abs(info["incremental_iou"]) < 1e-12
