@@ -12,7 +12,7 @@ from typing import Optional
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmpm_gb300.so")
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 MPM_OK = 0
 STATUS_OUT_OF_GRID = 1
 STATUS_NONFINITE = 2
@@ -36,11 +36,11 @@ class MpmParams(ctypes.Structure):
 
 
 class MpmToolDesc(ctypes.Structure):
-    _fields_ = [("type", _i32), ("action_dim", _i32), ("scene", _i32), ("reserved", _i32),
+    _fields_ = [("type", _i32), ("action_dim", _i32), ("scene", _i32), ("collision_mask", _i32),
                 ("friction", _f64), ("softness", _f64), ("radius", _f64), ("cap_h", _f64), ("cap_r", _f64),
                 ("size", _f64 * 3), ("prism_h", _f64 * 2), ("prot", _f64 * 4),
                 ("min_gap", _f64), ("max_gap", _f64), ("lower", _f64 * 3), ("upper", _f64 * 3),
-                ("action_scale", _f64 * 7)]
+                ("action_scale", _f64 * 7), ("torus", _f64 * 2)]
 
 
 class MpmGridStore(ctypes.Structure):
@@ -54,8 +54,10 @@ SIGNATURES = {
     "mpm_create": (_i32, [ctypes.POINTER(MpmParams), ctypes.POINTER(_i64), ctypes.POINTER(_c_p)]),
     "mpm_destroy": (_i32, [_c_p]),
     "mpm_set_tools": (_i32, [_c_p, ctypes.POINTER(MpmToolDesc), _i32]),
-    "mpm_tools_action": (_i32, [_c_p, _c_p, _c_p, _c_p, _i32, _c_p]),
-    "mpm_tools_action_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _i32, _c_p]),
+    "mpm_set_collision_points": (_i32, [_c_p, _c_p, _i32]),
+    "mpm_collision_pairs": (_i32, [_c_p]),
+    "mpm_tools_action": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _i32, _c_p]),
+    "mpm_tools_action_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _i32, _c_p]),
     "mpm_substep_fwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_substep_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_substep_fwd_store": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, ctypes.POINTER(MpmGridStore), _i32, _c_p]),

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 REPO = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "libmpm_gb300.so")
 BUILD_DIR = os.path.join(HERE, "_build")
-SOURCES = ["mpm_capi.cu", "mpm_fwd.cu", "mpm_bwd.cu", "mpm_loss.cu", "mpm_static.cu"]
+SOURCES = ["mpm_capi.cu", "mpm_fwd.cu", "mpm_bwd.cu", "mpm_loss.cu", "mpm_kinematics.cu", "mpm_static.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -22,8 +22,21 @@ TOOL_CAPSULE = 1
 TOOL_BOX = 2
 TOOL_KNIFE = 3
 TOOL_GRIPPER = 4
+TOOL_ROLLINGPIN = 5
+TOOL_ROLLINGPINEXT = 6
+TOOL_CHOPSTICKS = 7
+TOOL_CYLINDER = 8
+TOOL_TORUS = 9
+TOOL_GRIPPER2 = 10
 SHAPE_CODES = {"Sphere": TOOL_SPHERE, "Capsule": TOOL_CAPSULE, "Box": TOOL_BOX,
-               "Knife": TOOL_KNIFE, "Gripper": TOOL_GRIPPER}
+               "Knife": TOOL_KNIFE, "Gripper": TOOL_GRIPPER, "RollingPin": TOOL_ROLLINGPIN,
+               "RollingPinExt": TOOL_ROLLINGPINEXT, "Chopsticks": TOOL_CHOPSTICKS, "Cylinder": TOOL_CYLINDER,
+               "Torus": TOOL_TORUS, "Gripper2": TOOL_GRIPPER2}
+# tools whose state carries a gap (state_dim 8)
+GAP_SHAPES = ("Gripper", "Chopsticks", "Gripper2")
+# per-shape default_config values that differ from the Capsule defaults
+# (Cylinder primitives.py:323-326, Gripper2 688-697)
+SHAPE_DEFAULTS = {"Cylinder": {"h": 0.2, "r": 0.1}, "Gripper2": {"r": 0.015}}
 
 # Precision modes shared with the C ABI (MPM_PREC_*)
 PREC_FP32 = 0        # state, grid and SVD in FP32; reductions in FP64
@@ -120,11 +133,16 @@ class ActionConfig:
 class PrimitiveConfig:
     """One rigid tool (``cfg.PRIMITIVES`` entry).
 
-    ``shape`` is one of Sphere, Capsule, Box, Knife, Gripper.  Sizes follow
-    the reference's fields: ``radius`` (Sphere), ``h``/``r`` (Capsule,
-    segment along local y of length h), ``size`` (Box half extents; Knife box;
-    Gripper finger), ``prism_h``/``prot`` (Knife prism, the reference's
-    ``h``/``prot``), ``minimal_gap``/``maximal_gap``/``init_gap`` (Gripper).
+    ``shape`` is one of Sphere, Capsule, Box, Knife, Gripper, RollingPin,
+    RollingPinExt, Chopsticks, Cylinder, Torus, Gripper2.  Sizes follow the
+    reference's fields: ``radius`` (Sphere), ``h``/``r`` (Capsule segment along
+    local y of length h, also RollingPin(Ext), Chopsticks and the Gripper2
+    fingers; Cylinder radial extent h and half height r), ``size`` (Box half
+    extents; Knife box; Gripper finger), ``prism_h``/``prot`` (Knife prism, the
+    reference's ``h``/``prot``), ``tx``/``ty`` (Torus),
+    ``minimal_gap``/``maximal_gap``/``init_gap`` (Gripper, Chopsticks,
+    Gripper2), ``collision_group`` (entry j > 0: project this tool out of tool
+    j after every kinematics step, mpm_simulator.py:69-80).
     """
 
     shape: str = "Sphere"
@@ -143,6 +161,9 @@ class PrimitiveConfig:
     minimal_gap: float = 0.06
     maximal_gap: float = 1.0
     init_gap: float = 0.06
+    tx: float = 0.2
+    ty: float = 0.1
+    collision_group: Tuple[float, ...] = ()
 
     @property
     def type_code(self) -> int:
@@ -152,12 +173,17 @@ class PrimitiveConfig:
 
     @property
     def state_dim(self) -> int:
-        return 8 if self.shape == "Gripper" else 7
+        return 8 if self.shape in GAP_SHAPES else 7
 
     @property
     def init_state(self) -> Tuple[float, ...]:
         st = tuple(self.init_pos) + tuple(self.init_rot)
-        return st + ((self.init_gap,) if self.shape == "Gripper" else (0.0,))
+        return st + ((self.init_gap,) if self.shape in GAP_SHAPES else (0.0,))
+
+    @property
+    def collision_mask(self) -> int:
+        """Bit j set iff collision_group[j] > 0."""
+        return sum(1 << j for j, g in enumerate(self.collision_group) if float(g) > 0)
 
     def scale7(self) -> Tuple[float, ...]:
         s = list(self.action.scale) + [0.0] * (7 - len(self.action.scale))
@@ -169,6 +195,7 @@ def make_primitive(shape: str, **kw) -> PrimitiveConfig:
     action = kw.pop("action", None)
     if isinstance(action, dict):
         action = ActionConfig(dim=int(action.get("dim", 0)), scale=tuple(action.get("scale", ())))
+    kw = dict(SHAPE_DEFAULTS.get(shape, {}), **kw)
     cfg = PrimitiveConfig(shape=shape, **kw)
     if action is not None:
         cfg.action = action

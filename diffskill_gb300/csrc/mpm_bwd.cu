@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(128) k_tool_distance_adj(Consts<T> c, const T*
     PoseGrad<T> gP;
     gP.zero();
     bool any = false;
-    if (tl.type == TOOL_GRIPPER) {
+    if (fingered(tl.type)) {
 #pragma unroll
       for (int side = 0; side < 2; ++side) {
         T g = g_out[(int64_t)(col + side) * c.ld + p];
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(128) k_tool_distance_adj(Consts<T> c, const T*
         T flag = side == 0 ? T(-1) : T(1);
         T fp[3], gf[3] = {T(0), T(0), T(0)};
         finger_pos(P, flag, fp);
-        shape_sdf_vjp(tl, fp, P.rot, x, g, gx, gf, gP.rot);
+        shape_sdf_vjp(tl, fp, P.rot, T(0), x, g, gx, gf, gP.rot, (T*)nullptr);
         finger_pos_vjp(P, flag, gf, gP);
       }
     } else {

@@ -1,5 +1,5 @@
 // C ABI of the GB300 MPM substep (include/mpm_gb300.h): handle lifetime,
-// argument checks, precision dispatch, and the tool-kinematics kernels.
+// argument checks and precision dispatch.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -26,6 +26,11 @@ struct MpmHandle {
   std::vector<MpmToolDesc> h_tools;
   unsigned int* d_status = nullptr;
   int* d_flags = nullptr;  // convergence flags of mpm_target_sdf
+  int* d_pair_off = nullptr;  // [n_scenes + 1] first collision pair of each scene
+  int n_pairs = 0;            // tool-tool collision pairs over all scenes
+  int max_scene_pairs = 0;    // most pairs of one scene
+  double* d_coll_pts = nullptr;  // [n][600][3] random points of mpm_set_collision_points
+  int n_coll_pts = 0;            // pairs of points uploaded
   void* grid[4] = {nullptr, nullptr, nullptr, nullptr};
   unsigned char* d_blockbuf = nullptr;
   int* d_active = nullptr;
@@ -123,111 +128,11 @@ int check_aligned(MpmHandle* h, const void* ptr, const char* name, bool allow_nu
     if (_rc != MPM_OK) return _rc; \
   } while (0)
 
-// ---------------------------------------------------------------------------
-// tool kinematics (FP64): set_velocity + forward_kinematics per action
-// ---------------------------------------------------------------------------
-// wq = w2quat(vv[3..5]), computed once per action by the caller
-__device__ void fk_step(const MpmToolDesc& d, const double* p0, const double* vv, const double* wq, double* p1) {
-  for (int k = 0; k < 3; ++k) {
-    double a = p0[k] + vv[k];
-    double mn = (a < d.upper[k]) ? a : d.upper[k];
-    p1[k] = (d.lower[k] < mn) ? mn : d.lower[k];
-  }
-  if (d.type == mpm::TOOL_GRIPPER) {
-    mpm::qmul(p0 + 3, wq, p1 + 3);  // Gripper: rotation[f] * w2quat(w) (primitives.py:460)
-    double a = p0[7] - vv[6];
-    double mx = (d.min_gap < a) ? a : d.min_gap;
-    p1[7] = (mx < d.max_gap) ? mx : d.max_gap;
-  } else {
-    mpm::qmul(wq, p0 + 3, p1 + 3);  // w2quat(w) * rotation[f] (primive_base.py:156)
-    p1[7] = p0[7];
-  }
-}
-__device__ void action_velocity(const MpmToolDesc& d, const double* a, int n_sub, double* vv) {
-  for (int k = 0; k < 8; ++k) vv[k] = 0.0;
-  if (d.action_dim <= 0) return;
-  for (int k = 0; k < 3; ++k) vv[k] = a[k] * d.action_scale[k] / n_sub;
-  if (d.action_dim > 3)
-    for (int k = 0; k < 3; ++k) vv[3 + k] = a[3 + k] * d.action_scale[3 + k] / n_sub;
-  if (d.type == mpm::TOOL_GRIPPER) vv[6] = a[6] * d.action_scale[6] / n_sub;
-}
-__global__ void k_tools_action(const MpmToolDesc* __restrict__ tools, int n_tools, const double* __restrict__ action,
-                               double* __restrict__ vel, double* __restrict__ pose, int n_sub) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_tools) return;
-  const MpmToolDesc d = tools[t];
-  double vv[8], wq[4];
-  action_velocity(d, action + 8 * t, n_sub, vv);
-  mpm::w2quat(vv + 3, wq);  // the same for every substep of the action
-  for (int j = 0; j < n_sub; ++j) {
-    for (int k = 0; k < 8; ++k) vel[((int64_t)j * n_tools + t) * 8 + k] = vv[k];
-    fk_step(d, pose + ((int64_t)j * n_tools + t) * 8, vv, wq, pose + ((int64_t)(j + 1) * n_tools + t) * 8);
-  }
-}
-__global__ void k_tools_action_bwd(const MpmToolDesc* __restrict__ tools, int n_tools, const double* __restrict__ vel,
-                                   const double* __restrict__ pose, double* __restrict__ g_pose,
-                                   double* __restrict__ g_action, int n_sub) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_tools) return;
-  const MpmToolDesc d = tools[t];
-  double gvv_sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  // w2quat and its adjoint are evaluated once per run of substeps with the
-  // same angular velocity (set_velocity writes one per action): the
-  // quaternion gradient is summed over the run first (w2quat_vjp is linear in it)
-  double w_run[3] = {0, 0, 0}, wq[4] = {1, 0, 0, 0}, gwq_run[4] = {0, 0, 0, 0};
-  bool have_run = false;
-  for (int j = n_sub - 1; j >= 0; --j) {
-    const double* p0 = pose + ((int64_t)j * n_tools + t) * 8;
-    const double* vv = vel + ((int64_t)j * n_tools + t) * 8;
-    const double* g1 = g_pose + ((int64_t)(j + 1) * n_tools + t) * 8;
-    double* g0 = g_pose + ((int64_t)j * n_tools + t) * 8;
-    if (!have_run || vv[3] != w_run[0] || vv[4] != w_run[1] || vv[5] != w_run[2]) {
-      if (have_run) mpm::w2quat_vjp(w_run, gwq_run, gvv_sum + 3);
-      for (int k = 0; k < 3; ++k) w_run[k] = vv[3 + k];
-      for (int k = 0; k < 4; ++k) gwq_run[k] = 0.0;
-      mpm::w2quat(w_run, wq);
-      have_run = true;
-    }
-    double gvv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (int k = 0; k < 3; ++k) {
-      double a = p0[k] + vv[k];
-      double mn = (a < d.upper[k]) ? a : d.upper[k];
-      if ((a < d.upper[k]) && (d.lower[k] < mn)) {
-        g0[k] += g1[k];
-        gvv[k] += g1[k];
-      }
-    }
-    double gwq[4] = {0, 0, 0, 0};
-    if (d.type == mpm::TOOL_GRIPPER) {
-      mpm::qmul_vjp(p0 + 3, wq, g1 + 3, g0 + 3, gwq);
-      double a = p0[7] - vv[6];
-      double mx = (d.min_gap < a) ? a : d.min_gap;
-      if ((d.min_gap < a) && (mx < d.max_gap)) {
-        g0[7] += g1[7];
-        gvv[6] -= g1[7];
-      }
-    } else {
-      mpm::qmul_vjp(wq, p0 + 3, g1 + 3, gwq, g0 + 3);
-      g0[7] += g1[7];
-    }
-    for (int k = 0; k < 4; ++k) gwq_run[k] += gwq[k];
-    for (int k = 0; k < 8; ++k) gvv_sum[k] += gvv[k];
-  }
-  if (have_run) mpm::w2quat_vjp(w_run, gwq_run, gvv_sum + 3);
-  // set_velocity.grad: v = a * scale / n_sub for every substep of the action
-  if (d.action_dim > 0) {
-    for (int k = 0; k < 3; ++k) g_action[8 * t + k] += gvv_sum[k] * d.action_scale[k] / n_sub;
-    if (d.action_dim > 3)
-      for (int k = 0; k < 3; ++k) g_action[8 * t + 3 + k] += gvv_sum[3 + k] * d.action_scale[3 + k] / n_sub;
-    if (d.type == mpm::TOOL_GRIPPER) g_action[8 * t + 6] += gvv_sum[6] * d.action_scale[6] / n_sub;
-  }
-}
-
 }  // namespace
 
 extern "C" {
 
-const char* mpm_version(void) { return "mpm_gb300 1 (sm_103a)"; }
+const char* mpm_version(void) { return "mpm_gb300 2 (sm_103a)"; }
 
 int mpm_create(const MpmParams* params, const int64_t* scene_offsets, MpmHandle** out) {
   if (!params || !scene_offsets || !out) return fail(nullptr, MPM_E_INVALID, "mpm_create: NULL argument");
@@ -271,6 +176,7 @@ int mpm_create(const MpmParams* params, const int64_t* scene_offsets, MpmHandle*
   ok = ok && cudaMalloc(&h->d_tool_off, toff.size() * sizeof(int)) == cudaSuccess;
   ok = ok && cudaMalloc(&h->d_status, sizeof(unsigned int)) == cudaSuccess;
   ok = ok && cudaMalloc(&h->d_flags, 4 * sizeof(int)) == cudaSuccess;
+  ok = ok && cudaMalloc(&h->d_pair_off, toff.size() * sizeof(int)) == cudaSuccess;
   for (int i = 0; i < 4 && ok; ++i) ok = cudaMalloc(&h->grid[i], gbytes) == cudaSuccess;
   const int64_t nb = p.n_grid / 4;
   const int64_t nblocks = (int64_t)p.n_scenes * nb * nb * nb;
@@ -286,6 +192,7 @@ int mpm_create(const MpmParams* params, const int64_t* scene_offsets, MpmHandle*
   }
   if (!ps.empty()) e = cudaMemcpy(h->d_pscene, ps.data(), ps.size() * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(h->d_tool_off, toff.data(), toff.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(h->d_pair_off, toff.data(), toff.size() * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(h->d_status, 0, sizeof(unsigned int));
   if (e != cudaSuccess) {
     mpm_destroy(h);
@@ -303,6 +210,8 @@ int mpm_destroy(MpmHandle* h) {
   cudaFree(h->d_tools);
   cudaFree(h->d_status);
   cudaFree(h->d_flags);
+  cudaFree(h->d_pair_off);
+  cudaFree(h->d_coll_pts);
   for (int i = 0; i < 4; ++i) cudaFree(h->grid[i]);
   cudaFree(h->d_blockbuf);
   cudaFree(h->d_active);
@@ -319,7 +228,7 @@ int mpm_set_tools(MpmHandle* h, const MpmToolDesc* tools, int32_t n_tools) {
   int prev = 0;
   for (int i = 0; i < n_tools; ++i) {
     const MpmToolDesc& d = tools[i];
-    if (d.type < MPM_TOOL_SPHERE || d.type > MPM_TOOL_GRIPPER)
+    if (d.type < MPM_TOOL_SPHERE || d.type > MPM_TOOL_GRIPPER2)
       return fail(h, MPM_E_INVALID, "mpm_set_tools: tool " + std::to_string(i) + " has unknown type");
     if (d.scene < 0 || d.scene >= h->p.n_scenes || d.scene < prev)
       return fail(h, MPM_E_INVALID, "mpm_set_tools: tools must be sorted by a valid scene index");
@@ -334,11 +243,32 @@ int mpm_set_tools(MpmHandle* h, const MpmToolDesc* tools, int32_t n_tools) {
                                         " tools in scene " + std::to_string(s));
     toff[s + 1] += toff[s];
   }
+  // collision pairs (i, j) of each scene, scene-local indices, in the order
+  // of MPMSimulator.set_num_collision (mpm_simulator.py:69-80)
+  std::vector<int> poff(h->p.n_scenes + 1, 0);
+  int max_pairs = 0;
+  for (int s = 0; s < h->p.n_scenes; ++s) {
+    const int nt = toff[s + 1] - toff[s];
+    int np = 0;
+    for (int i = toff[s]; i < toff[s + 1]; ++i) {
+      const uint32_t m = (uint32_t)tools[i].collision_mask;
+      if (nt < 32 && (m >> nt) != 0)
+        return fail(h, MPM_E_INVALID, "mpm_set_tools: tool " + std::to_string(i) +
+                                          " has a collision_mask bit beyond its scene's tools");
+      for (int j = 0; j < nt; ++j)
+        if ((m >> j) & 1u) {
+          if (toff[s] + j == i) return fail(h, MPM_E_INVALID, "mpm_set_tools: a tool cannot collide with itself");
+          ++np;
+        }
+    }
+    poff[s + 1] = poff[s] + np;
+    max_pairs = std::max(max_pairs, np);
+  }
   std::vector<int> coff(std::max(n_tools, 1), 0);
   int ncols = 0;
   for (int i = 0; i < n_tools; ++i) {
     coff[i] = ncols;
-    ncols += tools[i].type == MPM_TOOL_GRIPPER ? 2 : 1;
+    ncols += (tools[i].type == MPM_TOOL_GRIPPER || tools[i].type == MPM_TOOL_GRIPPER2) ? 2 : 1;
   }
   cudaError_t e = cudaSuccess;
   if (n_tools > h->n_tools) {
@@ -355,13 +285,44 @@ int mpm_set_tools(MpmHandle* h, const MpmToolDesc* tools, int32_t n_tools) {
     e = cudaMemcpy(h->d_col_off, coff.data(), n_tools * sizeof(int), cudaMemcpyHostToDevice);
   h->n_cols = ncols;
   if (e == cudaSuccess) e = cudaMemcpy(h->d_tool_off, toff.data(), toff.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(h->d_pair_off, poff.data(), poff.size() * sizeof(int), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(h, e, "mpm_set_tools: upload");
+  h->n_pairs = poff[h->p.n_scenes];
+  h->max_scene_pairs = max_pairs;
   h->n_tools = n_tools;
   h->h_tools.assign(tools, tools + n_tools);
   return MPM_OK;
 }
 
-int mpm_tools_action(MpmHandle* h, const double* action, double* vel, double* pose, int32_t n_sub, void* stream) {
+int mpm_set_collision_points(MpmHandle* h, const double* points, int32_t n_pairs) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_set_collision_points: NULL handle");
+  if (n_pairs < 0 || (n_pairs > 0 && !points)) return fail(h, MPM_E_INVALID, "mpm_set_collision_points: bad array");
+  MPM_TRY(check_device(h));
+  cudaFree(h->d_coll_pts);
+  h->d_coll_pts = nullptr;
+  h->n_coll_pts = 0;
+  if (n_pairs == 0) return MPM_OK;
+  const size_t bytes = (size_t)n_pairs * 600 * 3 * sizeof(double);
+  cudaError_t e = cudaMalloc(&h->d_coll_pts, bytes);
+  if (e == cudaSuccess) e = cudaMemcpy(h->d_coll_pts, points, bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(h, e, "mpm_set_collision_points");
+  h->n_coll_pts = n_pairs;
+  return MPM_OK;
+}
+
+int mpm_collision_pairs(MpmHandle* h) { return h ? h->n_pairs : 0; }
+
+static int check_collision(MpmHandle* h, const double* coll, const char* what) {
+  if (h->n_pairs == 0) return MPM_OK;
+  if (h->n_coll_pts < h->max_scene_pairs)
+    return fail(h, MPM_E_INVALID, std::string(what) + ": a scene has " + std::to_string(h->max_scene_pairs) +
+                                      " collision pairs but mpm_set_collision_points gave points for " +
+                                      std::to_string(h->n_coll_pts));
+  return check_aligned(h, coll, "coll");
+}
+
+int mpm_tools_action(MpmHandle* h, const double* action, double* vel, double* pose, double* coll, int32_t n_sub,
+                     void* stream) {
   if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_tools_action: NULL handle");
   if (n_sub < 1) return fail(h, MPM_E_INVALID, "mpm_tools_action: n_sub must be >= 1");
   if (h->n_tools == 0) return MPM_OK;
@@ -369,15 +330,15 @@ int mpm_tools_action(MpmHandle* h, const double* action, double* vel, double* po
   MPM_TRY(check_aligned(h, action, "action"));
   MPM_TRY(check_aligned(h, vel, "vel"));
   MPM_TRY(check_aligned(h, pose, "pose"));
-  k_tools_action<<<(h->n_tools + 63) / 64, 64, 0, (cudaStream_t)stream>>>(h->d_tools, h->n_tools, action, vel, pose,
-                                                                          n_sub);
-  ++h->launches;
-  cudaError_t e = cudaGetLastError();
+  MPM_TRY(check_collision(h, coll, "mpm_tools_action"));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e = mpm::launch_tools_action(L, h->n_tools, h->d_pair_off, h->n_pairs, h->d_coll_pts, action, vel,
+                                           pose, coll, n_sub);
   return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_tools_action");
 }
 
-int mpm_tools_action_bwd(MpmHandle* h, const double* vel, const double* pose, double* g_pose, double* g_action,
-                         int32_t n_sub, void* stream) {
+int mpm_tools_action_bwd(MpmHandle* h, const double* vel, const double* pose, const double* coll, double* g_pose,
+                         double* g_action, int32_t n_sub, void* stream) {
   if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_tools_action_bwd: NULL handle");
   if (n_sub < 1) return fail(h, MPM_E_INVALID, "mpm_tools_action_bwd: n_sub must be >= 1");
   if (h->n_tools == 0) return MPM_OK;
@@ -386,10 +347,10 @@ int mpm_tools_action_bwd(MpmHandle* h, const double* vel, const double* pose, do
   MPM_TRY(check_aligned(h, pose, "pose"));
   MPM_TRY(check_aligned(h, g_pose, "g_pose"));
   MPM_TRY(check_aligned(h, g_action, "g_action"));
-  k_tools_action_bwd<<<(h->n_tools + 63) / 64, 64, 0, (cudaStream_t)stream>>>(h->d_tools, h->n_tools, vel, pose,
-                                                                              g_pose, g_action, n_sub);
-  ++h->launches;
-  cudaError_t e = cudaGetLastError();
+  MPM_TRY(check_collision(h, coll, "mpm_tools_action_bwd"));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e = mpm::launch_tools_action_bwd(L, h->n_tools, h->d_pair_off, h->n_pairs, h->d_coll_pts, vel, pose,
+                                               coll, g_pose, g_action, n_sub);
   return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_tools_action_bwd");
 }
 

@@ -183,12 +183,12 @@ __global__ void __launch_bounds__(128) k_tool_distance(Consts<T> c, const T* __r
     to_tool(tools[t], tl);
     to_pose(pose + 8 * t, P);
     const int col = col_off[t];
-    if (tl.type == TOOL_GRIPPER) {
+    if (fingered(tl.type)) {
       T fa[3], fb[3];
       finger_pos(P, T(-1), fa);
       finger_pos(P, T(1), fb);
-      out[(int64_t)col * c.ld + p] = shape_sdf(tl, fa, P.rot, x);
-      out[(int64_t)(col + 1) * c.ld + p] = shape_sdf(tl, fb, P.rot, x);
+      out[(int64_t)col * c.ld + p] = shape_sdf(tl, fa, P.rot, T(0), x);
+      out[(int64_t)(col + 1) * c.ld + p] = shape_sdf(tl, fb, P.rot, T(0), x);
     } else {
       out[(int64_t)col * c.ld + p] = tool_sdf(tl, P, x);
     }

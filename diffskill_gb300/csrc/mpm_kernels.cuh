@@ -440,30 +440,6 @@ struct SceneTools {
   Tool<T> tool[MAX_TOOLS_PER_SCENE];
   Pose<T> p0[MAX_TOOLS_PER_SCENE], p1[MAX_TOOLS_PER_SCENE];
 };
-template <typename T>
-MPM_DI void to_tool(const MpmToolDesc& d, Tool<T>& t) {
-  t.type = d.type;
-  t.action_dim = d.action_dim;
-  t.friction = T(d.friction);
-  t.softness = T(d.softness);
-  t.radius = T(d.radius);
-  t.cap_h = T(d.cap_h);
-  t.cap_r = T(d.cap_r);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) t.size[k] = T(d.size[k]);
-  t.prism_h[0] = T(d.prism_h[0]);
-  t.prism_h[1] = T(d.prism_h[1]);
-  T pr[4] = {T(d.prot[0]), T(d.prot[1]), T(d.prot[2]), T(d.prot[3])};
-  conj_unit(pr, t.prot_inv);
-}
-template <typename T>
-MPM_DI void to_pose(const double* src, Pose<T>& P) {
-#pragma unroll
-  for (int k = 0; k < 3; ++k) P.pos[k] = T(src[k]);
-#pragma unroll
-  for (int k = 0; k < 4; ++k) P.rot[k] = T(src[3 + k]);
-  P.gap = T(src[7]);
-}
 // loads the tools of `scene` (all threads call; one barrier inside)
 template <typename T>
 MPM_DI void load_scene_tools(SceneTools<T>& sh, int scene, const MpmToolDesc* __restrict__ tools,

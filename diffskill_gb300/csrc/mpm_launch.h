@@ -1,5 +1,5 @@
 // Internal launch interface between the C ABI (mpm_capi.cu) and the kernel
-// translation units (mpm_fwd.cu, mpm_bwd.cu, mpm_loss.cu).
+// translation units (mpm_fwd.cu, mpm_bwd.cu, mpm_loss.cu, mpm_kinematics.cu).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -92,6 +92,13 @@ cudaError_t launch_tool_distance(const LaunchCtx& L, const int* col_off, int n_c
 template <typename T>
 cudaError_t launch_tool_distance_bwd(const LaunchCtx& L, const int* col_off, const T* st, const double* pose,
                                      const T* g_out, T* gst, double* g_pose);
+// tool kinematics of one action with collision projection (mpm_kinematics.cu)
+cudaError_t launch_tools_action(const LaunchCtx& L, int n_tools, const int* pair_off, int n_pairs,
+                                const double* coll_pts, const double* action, double* vel, double* pose, double* coll,
+                                int n_sub);
+cudaError_t launch_tools_action_bwd(const LaunchCtx& L, int n_tools, const int* pair_off, int n_pairs,
+                                    const double* coll_pts, const double* vel, const double* pose, const double* coll,
+                                    double* g_pose, double* g_action, int n_sub);
 template <typename T>
 cudaError_t launch_target_sdf(const LaunchCtx& L, int* flags, const T* dens, T* sdf, T* near, T* work, int n_iters);
 template <typename T>

@@ -11,6 +11,7 @@
 #include <stdint.h>
 
 #define MPM_DI __device__ __forceinline__
+#define MPM_HD __host__ __device__
 
 namespace mpm {
 

@@ -104,9 +104,21 @@ class MpmEngine:
             d.lower[:] = list(t.lower_bound)
             d.upper[:] = list(t.upper_bound)
             d.action_scale[:] = list(t.scale7())
+            d.torus[:] = [t.tx, t.ty]
+            d.collision_mask = t.collision_mask
         self._descs = descs
         with torch.cuda.device(self.device):
             _lib.check(self.lib.mpm_set_tools(self.h, descs, self.T), self.h, "mpm_set_tools")
+            self.n_pairs = int(self.lib.mpm_collision_pairs(self.h))
+            if self.n_pairs:
+                # rand_num of the collision projection: np.random.seed(42) then
+                # uniform(-1.5, 1.5, (n_pairs, 600, 3)) (mpm_simulator.py:89-96);
+                # a scene's pair c uses row c of the same stream
+                most = max(sum(bin(self.tool_cfgs[i].collision_mask).count("1") for i in idx)
+                           for idx in self.scene_tools)
+                pts = np.ascontiguousarray(np.random.RandomState(42).uniform(-1.5, 1.5, (most, 600, 3)))
+                _lib.check(self.lib.mpm_set_collision_points(self.h, pts.ctypes.data_as(ctypes.c_void_p), most),
+                           self.h, "mpm_set_collision_points")
         self.scene_action_dims = [action_dims([self.tool_cfgs[i] for i in idx]) for idx in self.scene_tools]
         self.pose0 = torch.tensor([list(t.init_state) for t in self.tool_cfgs] or np.zeros((0, 8)),
                                   dtype=torch.float64, device=self.device).reshape(self.T, 8)
@@ -163,13 +175,25 @@ class MpmEngine:
         return out
 
     # -------------------------------------------------------------- C calls
-    def tools_action(self, action: torch.Tensor, vel: torch.Tensor, pose: torch.Tensor) -> None:
-        _lib.check(self.lib.mpm_tools_action(self.h, _ptr(action), _ptr(vel), _ptr(pose), self.n_sub, _stream()),
-                   self.h, "mpm_tools_action")
+    def new_coll(self, n_actions: int = 1) -> Optional[torch.Tensor]:
+        """[n_actions, n_sub, n_pairs, 4] collision records (None without collision pairs)."""
+        if not self.n_pairs:
+            return None
+        return torch.zeros((n_actions, self.n_sub, self.n_pairs, 4), dtype=torch.float64, device=self.device)
 
-    def tools_action_bwd(self, vel, pose, g_pose, g_action) -> None:
-        _lib.check(self.lib.mpm_tools_action_bwd(self.h, _ptr(vel), _ptr(pose), _ptr(g_pose), _ptr(g_action),
-                                                 self.n_sub, _stream()), self.h, "mpm_tools_action_bwd")
+    def tools_action(self, action: torch.Tensor, vel: torch.Tensor, pose: torch.Tensor,
+                     coll: Optional[torch.Tensor] = None) -> None:
+        if self.n_pairs and coll is None:
+            raise ValueError("this scene batch has tool-tool collision pairs: pass a collision record (new_coll)")
+        _lib.check(self.lib.mpm_tools_action(self.h, _ptr(action), _ptr(vel), _ptr(pose), _ptr(coll), self.n_sub,
+                                             _stream()), self.h, "mpm_tools_action")
+
+    def tools_action_bwd(self, vel, pose, g_pose, g_action, coll: Optional[torch.Tensor] = None) -> None:
+        if self.n_pairs and coll is None:
+            raise ValueError("this scene batch has tool-tool collision pairs: pass the forward's collision record")
+        _lib.check(self.lib.mpm_tools_action_bwd(self.h, _ptr(vel), _ptr(pose), _ptr(coll), _ptr(g_pose),
+                                                 _ptr(g_action), self.n_sub, _stream()), self.h,
+                   "mpm_tools_action_bwd")
 
     def substep(self, st0, st1, pose_f, pose_f1, store: "GridStore" = None, slot: int = -1) -> None:
         if store is None:
@@ -386,6 +410,7 @@ class Horizon:
         self.acts = torch.zeros((self.A, T, 8), dtype=torch.float64, device=dev)
         self.g_pose = torch.zeros_like(self.pose)
         self.g_act = torch.zeros_like(self.acts)
+        self.coll = eng.new_coll(self.A)
         self.g = torch.zeros((2, N_ROWS, eng.ld), dtype=dt, device=dev)
         self.gm = torch.zeros((eng.S, eng.G), dtype=dt, device=dev)
         self.g_gm = torch.zeros_like(self.gm)
@@ -457,7 +482,8 @@ class Horizon:
             self.pose[0].copy_(eng.pose0 if pose0 is None else pose0)
             self.acts.copy_(actions)
             for s in range(self.A):
-                eng.tools_action(self.acts[s], self.vel[s * n], self.pose[s * n])
+                eng.tools_action(self.acts[s], self.vel[s * n], self.pose[s * n],
+                                 None if self.coll is None else self.coll[s])
         store = self.store if (self.store is not None and self.k == 1) else None
         if store is not None:
             store.reset()
@@ -536,6 +562,7 @@ class Horizon:
                 self._unsort_grad(cur, f0 // self.R - 1)
         if eng.T:
             for s in range(self.A - 1, -1, -1):
-                eng.tools_action_bwd(self.vel[s * n], self.pose[s * n], self.g_pose[s * n], self.g_act[s])
+                eng.tools_action_bwd(self.vel[s * n], self.pose[s * n], self.g_pose[s * n], self.g_act[s],
+                                     None if self.coll is None else self.coll[s])
         self.g_state0 = cur
         return self.g_act

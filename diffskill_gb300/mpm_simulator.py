@@ -93,6 +93,7 @@ class MPMSimulator:
         n_act = M // self.substeps + 1
         self._act = torch.zeros((n_act, T, 8), dtype=torch.float64, device=eng.device)
         self._g_act = torch.zeros_like(self._act)
+        self._coll = eng.new_coll(n_act)  # tool-tool collision records per action
         self.grid_m_t = torch.zeros((1, eng.G), dtype=eng.dtype, device=eng.device)
         self.grid_m_grad_t = torch.zeros_like(self.grid_m_t)
         self.cur = 0
@@ -124,13 +125,15 @@ class MPMSimulator:
             row[i, :d] = self._t64(action[dims[i]:dims[i + 1]])
         self._act[s].copy_(row)
         if eng.T:
-            eng.tools_action(self._act[s], self._vel[s * n], self._pose[s * n])
+            eng.tools_action(self._act[s], self._vel[s * n], self._pose[s * n],
+                             None if self._coll is None else self._coll[s])
 
     def _tools_action_bwd(self, s: int) -> None:
         if s in self._fk_bwd_done or not self._eng.T:
             return
         n = self.substeps
-        self._eng.tools_action_bwd(self._vel[s * n], self._pose[s * n], self._g_pose[s * n], self._g_act[s])
+        self._eng.tools_action_bwd(self._vel[s * n], self._pose[s * n], self._g_pose[s * n], self._g_act[s],
+                                   None if self._coll is None else self._coll[s])
         self._fk_bwd_done.add(s)
 
     def tool_sdf(self, t: int, f: int, points: np.ndarray) -> np.ndarray:

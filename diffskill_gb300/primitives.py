@@ -42,8 +42,7 @@ class Primitive:
 
     @property
     def init_state(self):
-        return tuple(self.cfg.init_pos) + tuple(self.cfg.init_rot) + (
-            (self.cfg.init_gap,) if self.cfg.shape == "Gripper" else ())
+        return tuple(self.cfg.init_state[:self.state_dim])
 
     # -- state (primive_base.py:164-191) ---------------------------------------
     def get_state(self, f: int) -> np.ndarray:

@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define MPM_ABI_VERSION 1
+#define MPM_ABI_VERSION 2
 
 /* return codes */
 #define MPM_OK 0
@@ -54,6 +54,12 @@ extern "C" {
 #define MPM_TOOL_BOX 2     /* Box      primitives.py:359-425 */
 #define MPM_TOOL_KNIFE 3   /* Knife = Prism ∩ Box, primitives.py:700-815 */
 #define MPM_TOOL_GRIPPER 4 /* Gripper  primitives.py:428-573 */
+#define MPM_TOOL_ROLLINGPIN 5    /* RollingPin    primitives.py:101-117 (Capsule shape) */
+#define MPM_TOOL_ROLLINGPINEXT 6 /* RollingPinExt primitives.py:120-135 (Capsule shape) */
+#define MPM_TOOL_CHOPSTICKS 7    /* Chopsticks    primitives.py:218-290 */
+#define MPM_TOOL_CYLINDER 8      /* Cylinder      primitives.py:293-326 */
+#define MPM_TOOL_TORUS 9         /* Torus         primitives.py:329-356 */
+#define MPM_TOOL_GRIPPER2 10     /* Gripper2      primitives.py:576-697 (Capsule fingers) */
 
 /* status bits (sticky; cleared by mpm_status with clear=1) */
 #define MPM_STATUS_OUT_OF_GRID 1u /* a particle stencil left the grid; it was skipped */
@@ -79,16 +85,21 @@ typedef struct MpmToolDesc {
   int32_t type;       /* MPM_TOOL_* */
   int32_t action_dim; /* cfg.action.dim */
   int32_t scene;      /* owning scene; tools must be sorted by scene */
-  int32_t reserved;
+  /* bit j set: collision_group[j] > 0, i.e. this tool is projected out of
+   * the scene's tool j (a Box) after every forward-kinematics step
+   * (mpm_simulator.py:69-80, 287-305); j counts the scene's tools from 0 */
+  int32_t collision_mask;
   double friction, softness;
   double radius;        /* Sphere */
-  double cap_h, cap_r;  /* Capsule */
+  double cap_h, cap_r;  /* h, r: Capsule, RollingPin(Ext), Chopsticks, Gripper2 fingers;
+                           Cylinder: h = radial extent, r = half height (primitives.py:300-304) */
   double size[3];       /* Box / Knife box / Gripper finger half extents */
   double prism_h[2];    /* Knife prism h */
   double prot[4];       /* Knife prism rotation */
   double min_gap, max_gap;
   double lower[3], upper[3];
   double action_scale[7];
+  double torus[2];      /* Torus tx, ty */
 } MpmToolDesc;
 
 /* Grid store (caller-owned device buffers): the forward grid of a substep,
@@ -122,19 +133,40 @@ int mpm_destroy(MpmHandle* h);
  * tools: host array, sorted by scene; copied to the device. */
 int mpm_set_tools(MpmHandle* h, const MpmToolDesc* tools, int32_t n_tools);
 
+/* The random numbers of the tool-tool collision projection: points[c][k][3]
+ * for the c-th collision pair of a scene (c < n_pairs) and k < 600, drawn as
+ * the reference draws rand_num (np.random.seed(42); uniform(-1.5, 1.5,
+ * (n_pairs, 600, 3)), mpm_simulator.py:89-96).  Host array, copied.  Needed
+ * when any tool has a collision_mask. */
+int mpm_set_collision_points(MpmHandle* h, const double* points, int32_t n_pairs);
+/* Number of collision pairs over all scenes (rows of a coll record). */
+int mpm_collision_pairs(MpmHandle* h);
+
 /* Primitive.set_action + set_velocity + forward_kinematics for the n_sub
- * substeps of one action (primive_base.py:152-156, 246-274; Gripper
- * primitives.py:457-469).  action: double[n_tools][8] (clipped by the caller);
- * vel: double[n_sub][n_tools][8] written; pose: double[n_sub+1][n_tools][8]
- * with frame 0 given, frames 1..n_sub written.  One launch. */
-int mpm_tools_action(MpmHandle* h, const double* action, double* vel, double* pose, int32_t n_sub,
+ * substeps of one action (primive_base.py:152-156, 246-274; per-type
+ * kinematics of primitives.py: RollingPin 104-117, RollingPinExt 122-135,
+ * Chopsticks 231-245, Gripper 457-469, Gripper2 589-601), each substep
+ * followed by the tool-tool collision projection of MPMSimulator.substep
+ * (mpm_simulator.py:287-305, 316-319): every pair (i, j) takes the first of
+ * 600 points of box j's surface with the most negative SDF of tool i (none
+ * if no SDF is below 0) and moves tool i by normalized(normal) * SDF there.
+ * action: double[n_tools][8] (clipped by the caller); vel:
+ * double[n_sub][n_tools][8] written; pose: double[n_sub+1][n_tools][8] with
+ * frame 0 given, frames 1..n_sub written; coll: double[n_sub][n_pairs][4]
+ * written (chosen point index or -1, then the point), NULL if there are no
+ * collision pairs.  One launch; the 600 points are evaluated in parallel and
+ * the lowest index wins ties. */
+int mpm_tools_action(MpmHandle* h, const double* action, double* vel, double* pose, double* coll, int32_t n_sub,
                      void* stream);
-/* Adjoint: set_velocity.grad + forward_kinematics.grad (function.py:180-182).
+/* Adjoint: set_velocity.grad + forward_kinematics.grad (function.py:180-182)
+ * and, per substep before them, apply_collision_projection.grad and
+ * set_surface_points.grad (mpm_simulator.py:337-339), evaluated like the
+ * reference's autodiff at the stored (projected) poses and stored points.
  * g_pose: double[n_sub+1][n_tools][8] accumulated gradients of every frame on
  * entry; on exit g_pose[0] also holds what reaches frame 0.  g_action:
  * double[n_tools][8] accumulated. */
-int mpm_tools_action_bwd(MpmHandle* h, const double* vel, const double* pose, double* g_pose, double* g_action,
-                         int32_t n_sub, void* stream);
+int mpm_tools_action_bwd(MpmHandle* h, const double* vel, const double* pose, const double* coll, double* g_pose,
+                         double* g_action, int32_t n_sub, void* stream);
 
 /* One substep (MPMSimulator.substep, mpm_simulator.py:307-323, without the
  * forward_kinematics that mpm_tools_action already ran): clear_grid,

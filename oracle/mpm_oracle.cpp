@@ -48,7 +48,8 @@ struct OracleSim {
 };
 
 struct OracleTool {
-  int32_t type;  // 0 sphere, 1 capsule, 2 box, 3 knife, 4 gripper
+  int32_t type;  // 0 sphere, 1 capsule, 2 box, 3 knife, 4 gripper, 5 rolling pin, 6 rolling pin ext,
+                 // 7 chopsticks, 8 cylinder, 9 torus, 10 gripper2
   int32_t action_dim;
   double friction;
   double softness;
@@ -60,13 +61,30 @@ struct OracleTool {
   double min_gap, max_gap;
   double lower[3], upper[3];
   double action_scale[7];
+  double torus[2];         // Torus tx, ty
+  int32_t collision_mask;  // bit j: projected out of tool j (collision_group[j] > 0)
+  int32_t pad1;
 };
 
 }  // extern "C"
 
 namespace {
 
-enum { T_SPHERE = 0, T_CAPSULE = 1, T_BOX = 2, T_KNIFE = 3, T_GRIPPER = 4 };
+enum {
+  T_SPHERE = 0,
+  T_CAPSULE = 1,
+  T_BOX = 2,
+  T_KNIFE = 3,
+  T_GRIPPER = 4,
+  T_ROLLINGPIN = 5,
+  T_ROLLINGPINEXT = 6,
+  T_CHOPSTICKS = 7,
+  T_CYLINDER = 8,
+  T_TORUS = 9,
+  T_GRIPPER2 = 10
+};
+inline bool is_fingered(int type) { return type == T_GRIPPER || type == T_GRIPPER2; }
+inline bool has_gap_vel(int type) { return type == T_GRIPPER || type == T_CHOPSTICKS || type == T_GRIPPER2; }
 
 // ----------------------------------------------------------------------------
 // small linear algebra
@@ -255,7 +273,7 @@ inline void w2quat_vjp(const double* aa, const double* g, double* gaa) {
 // ----------------------------------------------------------------------------
 // local shape SDFs: plb/engine/primitive/primitives.py
 // ----------------------------------------------------------------------------
-enum { K_SPHERE = 0, K_CAPSULE = 1, K_BOX = 2, K_KNIFE = 3 };
+enum { K_SPHERE = 0, K_CAPSULE = 1, K_BOX = 2, K_KNIFE = 3, K_CHOPSTICKS = 4, K_CYLINDER = 5, K_TORUS = 6 };
 const double kFdStep = (double)(float)1e-4;  // d = ti.cast(1e-4, ti.float32) (primitives.py:385)
 
 // Capsule (primitives.py:55-66)
@@ -334,7 +352,137 @@ inline void knife_sdf_grad(const OracleTool& t, const double* q, double g, doubl
   else box_sdf_grad(t.size, q, g, gq);
 }
 
-inline double local_sdf(const OracleTool& t, int kind, const double* q) {
+// Chopsticks, Cylinder and Torus: value and derivatives by forward-mode dual
+// numbers with tangents (q0, q1, q2, gap).  Branches compare values, as the
+// reference's autodiff freezes them.
+struct Dual {
+  double v;
+  double d[4];
+  Dual(double c = 0.0) : v(c), d{0, 0, 0, 0} {}
+};
+inline Dual seed(double c, int k) {
+  Dual r(c);
+  r.d[k] = 1.0;
+  return r;
+}
+inline Dual operator+(const Dual& a, const Dual& b) {
+  Dual r(a.v + b.v);
+  for (int k = 0; k < 4; ++k) r.d[k] = a.d[k] + b.d[k];
+  return r;
+}
+inline Dual operator-(const Dual& a, const Dual& b) {
+  Dual r(a.v - b.v);
+  for (int k = 0; k < 4; ++k) r.d[k] = a.d[k] - b.d[k];
+  return r;
+}
+inline Dual operator*(const Dual& a, const Dual& b) {
+  Dual r(a.v * b.v);
+  for (int k = 0; k < 4; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+  return r;
+}
+inline Dual operator/(const Dual& a, const Dual& b) {
+  Dual r(a.v / b.v);
+  for (int k = 0; k < 4; ++k) r.d[k] = (a.d[k] * b.v - a.v * b.d[k]) / (b.v * b.v);
+  return r;
+}
+inline Dual dsqrt(const Dual& a) {
+  Dual r(std::sqrt(a.v));
+  for (int k = 0; k < 4; ++k) r.d[k] = a.d[k] / (2.0 * r.v);
+  return r;
+}
+inline Dual dabs(const Dual& a) {  // abs' = sgn, 0 at 0
+  Dual r(std::fabs(a.v));
+  for (int k = 0; k < 4; ++k) r.d[k] = a.d[k] * sgn(a.v);
+  return r;
+}
+inline Dual dlen(const Dual& a, const Dual& b) { return dsqrt(a * a + b * b + Dual(1e-14)); }
+inline Dual dlen(const Dual& a, const Dual& b, const Dual& c) { return dsqrt(a * a + b * b + c * c + Dual(1e-14)); }
+inline Dual dmax0(const Dual& a) { return (0.0 < a.v) ? a : Dual(0.0); }  // max(a, 0)
+
+// Capsule._sdf on (x, y, z) with the segment [-h/2, h/2] on y (primitives.py:55-60)
+inline Dual capsule_y(double h, const Dual& y) {
+  Dual a = y + Dual(h / 2);
+  Dual m1 = (0.0 < a.v) ? a : Dual(0.0);
+  Dual m2 = (m1.v < h) ? m1 : Dual(h);
+  return a - m2;
+}
+// Chopsticks._sdf (primitives.py:248-254): min of capsules at x -+ gap/2 around q + (0, h/2, 0)
+inline Dual chop_sdf(const OracleTool& t, const Dual* q, const Dual& gap, bool* first) {
+  Dual half = gap / Dual(2.0);
+  Dual y = capsule_y(t.cap_h, q[1] + Dual(t.cap_h / 2));
+  Dual xa = q[0] - half, xb = q[0] + half;
+  Dual a = dlen(xa, y, q[2]) - Dual(t.cap_r), b = dlen(xb, y, q[2]) - Dual(t.cap_r);
+  if (first) *first = a.v <= b.v;
+  return (a.v < b.v) ? a : b;
+}
+inline void chop_normal(const OracleTool& t, const Dual* q, const Dual& gap, Dual* n) {
+  bool first;
+  chop_sdf(t, q, gap, &first);  // Chopsticks._normal (256-266): normal of the capsule with a <= b
+  Dual half = gap / Dual(2.0);
+  Dual x = first ? q[0] - half : q[0] + half;
+  Dual y = capsule_y(t.cap_h, q[1] + Dual(t.cap_h / 2));
+  Dual L = dlen(x, y, q[2]);
+  n[0] = x / L;
+  n[1] = y / L;
+  n[2] = q[2] / L;
+}
+// Cylinder._sdf (primitives.py:300-303)
+inline Dual cyl_sdf(const OracleTool& t, const Dual* q) {
+  Dual d0 = dabs(dlen(q[0], q[2])) - Dual(t.cap_h);
+  Dual d1 = dabs(q[1]) - Dual(t.cap_r);
+  Dual mx = (d1.v < d0.v) ? d0 : d1;
+  Dual in = (mx.v < 0.0) ? mx : Dual(0.0);
+  return in + dlen(dmax0(d0), dmax0(d1));
+}
+// Cylinder._normal (primitives.py:306-321)
+inline void cyl_normal(const OracleTool& t, const Dual* q, Dual* n) {
+  Dual l = dlen(q[0], q[2]);
+  Dual d0 = l - Dual(t.cap_h), d1 = dabs(q[1]) - Dual(t.cap_r);
+  double f = (d0.v > d1.v) ? 1.0 : 0.0;
+  double inside = (std::max(d0.v, d1.v) <= 0.0) ? 1.0 : 0.0;
+  Dual a0 = dmax0(d0) + Dual(inside * f), a1 = dmax0(d1) + Dual(inside * (1.0 - f));
+  Dual L2 = dlen(a0, a1);
+  Dual n0 = a0 / L2, n1 = a1 / L2;
+  double sy = (q[1].v >= 0.0) ? 1.0 : -1.0;
+  Dual m0 = q[0] / l * n0, m1 = n1 * Dual(sy), m2 = q[2] / l * n0;
+  Dual L3 = dlen(m0, m1, m2);
+  n[0] = m0 / L3;
+  n[1] = m1 / L3;
+  n[2] = m2 / L3;
+}
+// Torus._sdf / _normal (primitives.py:336-350)
+inline Dual torus_sdf(const OracleTool& t, const Dual* q) {
+  return dlen(dlen(q[0], q[2]) - Dual(t.torus[0]), q[1]) - Dual(t.torus[1]);
+}
+inline void torus_normal(const OracleTool& t, const Dual* q, Dual* n) {
+  Dual l = dlen(q[0], q[2]);
+  Dual qa = dlen(q[0], q[2]) - Dual(t.torus[0]);
+  Dual Lq = dlen(qa, q[1]);
+  Dual n0 = qa / Lq, n1 = q[1] / Lq;
+  Dual m0 = q[0] / l * n0, m2 = q[2] / l * n0;
+  Dual L3 = dlen(m0, n1, m2);
+  n[0] = m0 / L3;
+  n[1] = n1 / L3;
+  n[2] = m2 / L3;
+}
+inline Dual dual_sdf(const OracleTool& t, int kind, const double* q, double gap) {
+  Dual qd[3] = {seed(q[0], 0), seed(q[1], 1), seed(q[2], 2)};
+  Dual g = seed(gap, 3);
+  if (kind == K_CHOPSTICKS) return chop_sdf(t, qd, g, nullptr);
+  if (kind == K_CYLINDER) return cyl_sdf(t, qd);
+  return torus_sdf(t, qd);
+}
+inline void dual_normal(const OracleTool& t, int kind, const double* q, double gap, Dual* n) {
+  Dual qd[3] = {seed(q[0], 0), seed(q[1], 1), seed(q[2], 2)};
+  Dual g = seed(gap, 3);
+  if (kind == K_CHOPSTICKS) chop_normal(t, qd, g, n);
+  else if (kind == K_CYLINDER) cyl_normal(t, qd, n);
+  else torus_normal(t, qd, n);
+}
+inline bool is_dual_kind(int kind) { return kind == K_CHOPSTICKS || kind == K_CYLINDER || kind == K_TORUS; }
+
+inline double local_sdf(const OracleTool& t, int kind, const double* q, double gap) {
+  if (is_dual_kind(kind)) return dual_sdf(t, kind, q, gap).v;
   switch (kind) {
     case K_CAPSULE: {
       double p2[3], dp;
@@ -345,7 +493,14 @@ inline double local_sdf(const OracleTool& t, int kind, const double* q) {
     default: return knife_sdf(t, q);
   }
 }
-inline void local_sdf_grad(const OracleTool& t, int kind, const double* q, double g, double* gq) {
+inline void local_sdf_grad(const OracleTool& t, int kind, const double* q, double gap, double g, double* gq,
+                           double* ggap) {
+  if (is_dual_kind(kind)) {
+    Dual r = dual_sdf(t, kind, q, gap);
+    for (int k = 0; k < 3; ++k) gq[k] += g * r.d[k];
+    if (ggap) *ggap += g * r.d[3];
+    return;
+  }
   switch (kind) {
     case K_CAPSULE: {
       double p2[3], dp;
@@ -366,10 +521,16 @@ inline void fd_normal_raw(const OracleTool& t, int kind, const double* q, double
     double inc[3] = {q[0], q[1], q[2]}, dec[3] = {q[0], q[1], q[2]};
     inc[i] += kFdStep;
     dec[i] -= kFdStep;
-    n[i] = (0.5 / kFdStep) * (local_sdf(t, kind, inc) - local_sdf(t, kind, dec));
+    n[i] = (0.5 / kFdStep) * (local_sdf(t, kind, inc, 0.0) - local_sdf(t, kind, dec, 0.0));
   }
 }
-inline void local_normal(const OracleTool& t, int kind, const double* q, double* n) {
+inline void local_normal(const OracleTool& t, int kind, const double* q, double gap, double* n) {
+  if (is_dual_kind(kind)) {
+    Dual nd[3];
+    dual_normal(t, kind, q, gap, nd);
+    for (int k = 0; k < 3; ++k) n[k] = nd[k].v;
+    return;
+  }
   if (kind == K_CAPSULE) {
     double p2[3], dp;
     capsule_p2(t, q, p2, &dp);
@@ -388,7 +549,15 @@ inline void unit14_vjp(const double* u, const double* g, double* gu) {
   double ug = dot3(u, g);
   for (int k = 0; k < 3; ++k) gu[k] = g[k] / L - u[k] * ug / (L * L * L);
 }
-inline void local_normal_vjp(const OracleTool& t, int kind, const double* q, const double* gn, double* gq) {
+inline void local_normal_vjp(const OracleTool& t, int kind, const double* q, double gap, const double* gn,
+                             double* gq, double* ggap) {
+  if (is_dual_kind(kind)) {
+    Dual nd[3];
+    dual_normal(t, kind, q, gap, nd);
+    for (int k = 0; k < 3; ++k) gq[k] += gn[0] * nd[0].d[k] + gn[1] * nd[1].d[k] + gn[2] * nd[2].d[k];
+    if (ggap) *ggap += gn[0] * nd[0].d[3] + gn[1] * nd[1].d[3] + gn[2] * nd[2].d[3];
+    return;
+  }
   if (kind == K_CAPSULE) {
     double p2[3], dp;
     capsule_p2(t, q, p2, &dp);
@@ -408,8 +577,8 @@ inline void local_normal_vjp(const OracleTool& t, int kind, const double* q, con
     inc[i] += kFdStep;
     dec[i] -= kFdStep;
     double c = (0.5 / kFdStep) * gr[i];
-    local_sdf_grad(t, kind, inc, c, gq);
-    local_sdf_grad(t, kind, dec, -c, gq);
+    local_sdf_grad(t, kind, inc, 0.0, c, gq, nullptr);
+    local_sdf_grad(t, kind, dec, 0.0, -c, gq, nullptr);
   }
 }
 
@@ -419,10 +588,12 @@ inline void local_normal_vjp(const OracleTool& t, int kind, const double* q, con
 struct Pose {
   double pos[3];
   double rot[4];
+  double gap = 0.0;  // only the Chopsticks shape depends on it
 };
 struct PoseGrad {
   double pos[3] = {0, 0, 0};
   double rot[4] = {0, 0, 0, 0};
+  double gap = 0.0;
 };
 
 // Sphere.sdf / Sphere.normal (primitives.py:28-34): no rotation
@@ -434,7 +605,7 @@ inline double shape_sdf(const OracleTool& t, int kind, const Pose& P, const doub
   }
   double q[3];
   inv_trans(p, P.pos, P.rot, q);
-  return local_sdf(t, kind, q);
+  return local_sdf(t, kind, q, P.gap);
 }
 inline void shape_sdf_vjp(const OracleTool& t, int kind, const Pose& P, const double* p, double g, double* gp,
                           PoseGrad* gP) {
@@ -450,7 +621,7 @@ inline void shape_sdf_vjp(const OracleTool& t, int kind, const Pose& P, const do
   double q[3];
   inv_trans(p, P.pos, P.rot, q);
   double gq[3] = {0, 0, 0};
-  local_sdf_grad(t, kind, q, g, gq);
+  local_sdf_grad(t, kind, q, P.gap, g, gq, gP ? &gP->gap : nullptr);
   inv_trans_vjp(p, P.pos, P.rot, gq, gp, gP ? gP->pos : nullptr, gP ? gP->rot : nullptr);
 }
 inline void shape_normal(const OracleTool& t, int kind, const Pose& P, const double* p, double* n) {
@@ -462,26 +633,30 @@ inline void shape_normal(const OracleTool& t, int kind, const Pose& P, const dou
   }
   double q[3], nl[3];
   inv_trans(p, P.pos, P.rot, q);
-  local_normal(t, kind, q, nl);
+  local_normal(t, kind, q, P.gap, nl);
   qrot(P.rot, nl, n);
 }
+// gp (the point's gradient) may be null
 inline void shape_normal_vjp(const OracleTool& t, int kind, const Pose& P, const double* p, const double* gn,
-                             PoseGrad* gP) {
+                             PoseGrad* gP, double* gp = nullptr) {
   if (kind == K_SPHERE) {
     const double d[3] = {p[0] - P.pos[0], p[1] - P.pos[1], p[2] - P.pos[2]};
     double gd[3];
     unit14_vjp(d, gn, gd);
-    for (int k = 0; k < 3; ++k) gP->pos[k] -= gd[k];
+    for (int k = 0; k < 3; ++k) {
+      gP->pos[k] -= gd[k];
+      if (gp) gp[k] += gd[k];
+    }
     return;
   }
   double q[3], nl[3];
   inv_trans(p, P.pos, P.rot, q);
-  local_normal(t, kind, q, nl);
+  local_normal(t, kind, q, P.gap, nl);
   double gnl[3] = {0, 0, 0};
   qrot_vjp(P.rot, nl, gn, gP->rot, gnl);
   double gq[3] = {0, 0, 0};
-  local_normal_vjp(t, kind, q, gnl, gq);
-  inv_trans_vjp(p, P.pos, P.rot, gq, nullptr, gP->pos, gP->rot);
+  local_normal_vjp(t, kind, q, P.gap, gnl, gq, &gP->gap);
+  inv_trans_vjp(p, P.pos, P.rot, gq, gp, gP->pos, gP->rot);
 }
 // collider_v (primive_base.py:87-94; Gripper.collider_v primitives.py:498-505)
 inline void collider_v(const Pose& P0, const Pose& P1, const double* p, double dt, double* cv) {
@@ -624,13 +799,25 @@ inline Pose rigid_pose(const double* pose8) {
   Pose P;
   for (int k = 0; k < 3; ++k) P.pos[k] = pose8[k];
   for (int k = 0; k < 4; ++k) P.rot[k] = pose8[3 + k];
+  P.gap = pose8[7];
   return P;
+}
+inline void add_pose_grad(const PoseGrad& g, double* gpose8) {
+  for (int k = 0; k < 3; ++k) gpose8[k] += g.pos[k];
+  for (int k = 0; k < 4; ++k) gpose8[3 + k] += g.rot[k];
+  gpose8[7] += g.gap;
 }
 inline int tool_kind(const OracleTool& t) {
   switch (t.type) {
     case T_SPHERE: return K_SPHERE;
-    case T_CAPSULE: return K_CAPSULE;
+    case T_CAPSULE:
+    case T_ROLLINGPIN:
+    case T_ROLLINGPINEXT:
+    case T_GRIPPER2: return K_CAPSULE;  // Gripper2 fingers are capsules
     case T_KNIFE: return K_KNIFE;
+    case T_CHOPSTICKS: return K_CHOPSTICKS;
+    case T_CYLINDER: return K_CYLINDER;
+    case T_TORUS: return K_TORUS;
     default: return K_BOX;  // box and gripper fingers
   }
 }
@@ -639,7 +826,7 @@ inline int tool_kind(const OracleTool& t) {
 inline void tool_collide(const OracleTool& t, const double* pose0, const double* pose1, const double* p, double dt,
                          const double* vin, double* vout) {
   int kind = tool_kind(t);
-  if (t.type == T_GRIPPER) {
+  if (is_fingered(t.type)) {
     double mid[3];
     collide_fwd(t, kind, finger_pose(pose0, -1), finger_pose(pose1, -1), p, dt, vin, mid, nullptr);
     collide_fwd(t, kind, finger_pose(pose0, 1), finger_pose(pose1, 1), p, dt, mid, vout, nullptr);
@@ -650,7 +837,7 @@ inline void tool_collide(const OracleTool& t, const double* pose0, const double*
 inline void tool_collide_vjp(const OracleTool& t, const double* pose0, const double* pose1, const double* p, double dt,
                              const double* vin, const double* gout, double* gvin, double* gpose0, double* gpose1) {
   int kind = tool_kind(t);
-  if (t.type == T_GRIPPER) {
+  if (is_fingered(t.type)) {
     double mid[3];
     Pose A0 = finger_pose(pose0, -1), A1 = finger_pose(pose1, -1);
     Pose B0 = finger_pose(pose0, 1), B1 = finger_pose(pose1, 1);
@@ -666,20 +853,14 @@ inline void tool_collide_vjp(const OracleTool& t, const double* pose0, const dou
   } else {
     PoseGrad g0, g1;
     collide_vjp(t, kind, rigid_pose(pose0), rigid_pose(pose1), p, dt, vin, gout, gvin, &g0, &g1);
-    for (int k = 0; k < 3; ++k) {
-      gpose0[k] += g0.pos[k];
-      gpose1[k] += g1.pos[k];
-    }
-    for (int k = 0; k < 4; ++k) {
-      gpose0[3 + k] += g0.rot[k];
-      gpose1[3 + k] += g1.rot[k];
-    }
+    add_pose_grad(g0, gpose0);
+    add_pose_grad(g1, gpose1);
   }
 }
 // world SDF of a tool (Gripper.sdf = min of fingers, primitives.py:486-487)
 inline double tool_sdf(const OracleTool& t, const double* pose, const double* p) {
   int kind = tool_kind(t);
-  if (t.type == T_GRIPPER) {
+  if (is_fingered(t.type)) {
     double a = shape_sdf(t, kind, finger_pose(pose, -1), p);
     double b = shape_sdf(t, kind, finger_pose(pose, 1), p);
     return (a < b) ? a : b;
@@ -689,7 +870,7 @@ inline double tool_sdf(const OracleTool& t, const double* pose, const double* p)
 inline void tool_sdf_vjp(const OracleTool& t, const double* pose, const double* p, double g, double* gp,
                          double* gpose) {
   int kind = tool_kind(t);
-  if (t.type == T_GRIPPER) {
+  if (is_fingered(t.type)) {
     Pose A = finger_pose(pose, -1), B = finger_pose(pose, 1);
     double a = shape_sdf(t, kind, A, p), b = shape_sdf(t, kind, B, p);
     PoseGrad gF;
@@ -704,15 +885,12 @@ inline void tool_sdf_vjp(const OracleTool& t, const double* pose, const double* 
   }
   PoseGrad gP;
   shape_sdf_vjp(t, kind, rigid_pose(pose), p, g, gp, &gP);
-  if (gpose) {
-    for (int k = 0; k < 3; ++k) gpose[k] += gP.pos[k];
-    for (int k = 0; k < 4; ++k) gpose[3 + k] += gP.rot[k];
-  }
+  if (gpose) add_pose_grad(gP, gpose);
 }
 // world normal (Gripper.normal picks the nearer finger, primitives.py:489-496)
 inline void tool_normal(const OracleTool& t, const double* pose, const double* p, double* n) {
   int kind = tool_kind(t);
-  if (t.type == T_GRIPPER) {
+  if (is_fingered(t.type)) {
     Pose A = finger_pose(pose, -1), B = finger_pose(pose, 1);
     double a = shape_sdf(t, kind, A, p), b = shape_sdf(t, kind, B, p);
     double na[3], nb[3];
@@ -723,6 +901,21 @@ inline void tool_normal(const OracleTool& t, const double* pose, const double* p
     return;
   }
   shape_normal(t, kind, rigid_pose(pose), p, n);
+}
+inline void tool_normal_vjp(const OracleTool& t, const double* pose, const double* p, const double* gn, double* gp,
+                            double* gpose) {
+  int kind = tool_kind(t);
+  if (is_fingered(t.type)) {
+    Pose A = finger_pose(pose, -1), B = finger_pose(pose, 1);
+    double a = shape_sdf(t, kind, A, p), b = shape_sdf(t, kind, B, p);
+    PoseGrad gF;
+    shape_normal_vjp(t, kind, a <= b ? A : B, p, gn, &gF, gp);
+    finger_pose_vjp(pose, a <= b ? -1.0 : 1.0, gF, gpose);
+    return;
+  }
+  PoseGrad gP;
+  shape_normal_vjp(t, kind, rigid_pose(pose), p, gn, &gP, gp);
+  add_pose_grad(gP, gpose);
 }
 
 // ----------------------------------------------------------------------------
@@ -1170,13 +1363,13 @@ void oracle_tool_sdf_vjp(const OracleTool* tool, const double* pose, int64_t m, 
 // per-point distance columns of one tool (GradModel.compute_min_dist,
 // function.py:79-89): Gripper -> two columns (sdf_2 with flag -1, +1,
 // primitives.py:479-483), other tools -> one column (sdf).  out: [m][ncol].
-int oracle_tool_distance_cols(const OracleTool* tool) { return tool->type == T_GRIPPER ? 2 : 1; }
+int oracle_tool_distance_cols(const OracleTool* tool) { return is_fingered(tool->type) ? 2 : 1; }
 void oracle_tool_distance(const OracleTool* tool, const double* pose, int64_t m, const double* pts, double* out) {
   const int nc = oracle_tool_distance_cols(tool);
   for (int64_t i = 0; i < m; ++i) {
-    if (tool->type == T_GRIPPER) {
-      out[i * nc] = shape_sdf(*tool, K_BOX, finger_pose(pose, -1), pts + 3 * i);
-      out[i * nc + 1] = shape_sdf(*tool, K_BOX, finger_pose(pose, 1), pts + 3 * i);
+    if (is_fingered(tool->type)) {
+      out[i * nc] = shape_sdf(*tool, tool_kind(*tool), finger_pose(pose, -1), pts + 3 * i);
+      out[i * nc + 1] = shape_sdf(*tool, tool_kind(*tool), finger_pose(pose, 1), pts + 3 * i);
     } else {
       out[i * nc] = tool_sdf(*tool, pose, pts + 3 * i);
     }
@@ -1186,11 +1379,12 @@ void oracle_tool_distance_vjp(const OracleTool* tool, const double* pose, int64_
                               const double* g, double* g_pts, double* g_pose) {
   const int nc = oracle_tool_distance_cols(tool);
   for (int64_t i = 0; i < m; ++i) {
-    if (tool->type == T_GRIPPER) {
+    if (is_fingered(tool->type)) {
       for (int side = 0; side < 2; ++side) {
         double flag = side == 0 ? -1.0 : 1.0;
         PoseGrad gF;
-        shape_sdf_vjp(*tool, K_BOX, finger_pose(pose, flag), pts + 3 * i, g[i * nc + side], g_pts + 3 * i, &gF);
+        shape_sdf_vjp(*tool, tool_kind(*tool), finger_pose(pose, flag), pts + 3 * i, g[i * nc + side], g_pts + 3 * i,
+                      &gF);
         finger_pose_vjp(pose, flag, gF, g_pose);
       }
     } else {
@@ -1210,12 +1404,207 @@ void oracle_tool_collide_vjp(const OracleTool* tool, const double* pose0, const 
     tool_collide_vjp(*tool, pose0, pose1, pts + 3 * i, dt, vin + 3 * i, gout + 3 * i, gvin + 3 * i, gpose0, gpose1);
 }
 
-// Primitive.set_velocity (primive_base.py:260-268; Gripper 462-469) followed by
-// forward_kinematics (primive_base.py:152-156; Gripper 457-460) for the n_sub
-// substeps of one action.  pose: [(n_sub+1)][T][8] with frame 0 given.
-// vel: [n_sub][T][8] written.  action: [T][7] (already clipped to [-1, 1]).
-void oracle_tools_action(const OracleTool* tools, int T, int n_sub, const double* action, double* vel,
-                         double* pose) {
+// Primitive.set_velocity (primive_base.py:260-268; Gripper primitives.py:463-469,
+// Chopsticks 238-245, Gripper2 595-601) followed by forward_kinematics
+// (primive_base.py:153-156; RollingPin primitives.py:104-117, RollingPinExt
+// 122-135, Chopsticks 231-235, Gripper 457-460, Gripper2 589-592) and, when
+// tools have collision masks, the collision projection of every substep
+// (mpm_simulator.py:287-305, 316-319) for the n_sub substeps of one action.
+// pose: [(n_sub+1)][T][8] with frame 0 given.  vel: [n_sub][T][8] written.
+// action: [T][7] (already clipped to [-1, 1]).  pts: [n_pairs][600][3] random
+// numbers (rand_num); coll: [n_sub][n_pairs][4] written (index or -1, point).
+}  // extern "C"
+namespace {
+const int kSurfacePoints = 600;
+struct Pair {
+  int i, j;
+};
+std::vector<Pair> collision_pairs(const OracleTool* tools, int T) {
+  std::vector<Pair> pr;
+  for (int i = 0; i < T; ++i)
+    for (int j = 0; j < T; ++j)
+      if ((tools[i].collision_mask >> j) & 1) pr.push_back({i, j});
+  return pr;
+}
+inline void clamp_xyz(const OracleTool& tl, const double* p0, const double* dv, double* p1, bool* pass) {
+  for (int k = 0; k < 3; ++k) {
+    double a = p0[k] + dv[k];
+    double mn = (a < tl.upper[k]) ? a : tl.upper[k];
+    p1[k] = (tl.lower[k] < mn) ? mn : tl.lower[k];
+    pass[k] = (a < tl.upper[k]) && (tl.lower[k] < mn);
+  }
+}
+// RollingPin(Ext): x_dir = (0,1,0) x qrot(rot, (0,-1,0)) * (dw*0.03 [+ w0]), x_dir.y = dy
+inline void rolling_terms(const OracleTool& tl, const double* p0, const double* vv, double* yd, double* s,
+                          double* xd) {
+  const double down[3] = {0, -1, 0};
+  qrot(p0 + 3, down, yd);
+  *s = vv[0] * 0.03 + (tl.type == T_ROLLINGPINEXT ? vv[3] : 0.0);
+  const double up[3] = {0, 1, 0};
+  cross3(up, yd, xd);
+  for (int k = 0; k < 3; ++k) xd[k] *= *s;
+  xd[1] = vv[2];
+}
+void fk(const OracleTool& tl, const double* p0, const double* vv, double* p1) {
+  bool pass[3];
+  if (tl.type == T_ROLLINGPIN || tl.type == T_ROLLINGPINEXT) {
+    double yd[3], s, xd[3];
+    rolling_terms(tl, p0, vv, yd, &s, xd);
+    clamp_xyz(tl, p0, xd, p1, pass);
+    const double wa[3] = {0, -vv[1], 0}, wb[3] = {0, vv[0], 0};
+    double qa[4], qb[4], t[4];
+    w2quat(wa, qa);
+    w2quat(wb, qb);
+    qmul(p0 + 3, qb, t);
+    qmul(qa, t, p1 + 3);
+    p1[7] = p0[7];
+    return;
+  }
+  clamp_xyz(tl, p0, vv, p1, pass);
+  double wq[4];
+  w2quat(vv + 3, wq);
+  if (has_gap_vel(tl.type)) {
+    qmul(p0 + 3, wq, p1 + 3);
+    double a = p0[7] - vv[6];
+    double mx = (tl.min_gap < a) ? a : tl.min_gap;
+    p1[7] = (tl.type == T_CHOPSTICKS) ? mx : ((mx < tl.max_gap) ? mx : tl.max_gap);
+  } else {
+    qmul(wq, p0 + 3, p1 + 3);
+    p1[7] = p0[7];
+  }
+}
+void fk_vjp(const OracleTool& tl, const double* p0, const double* vv, const double* g1, double* g0, double* gvv) {
+  bool pass[3];
+  double tmp[8];
+  if (tl.type == T_ROLLINGPIN || tl.type == T_ROLLINGPINEXT) {
+    double yd[3], s, xd[3];
+    rolling_terms(tl, p0, vv, yd, &s, xd);
+    clamp_xyz(tl, p0, xd, tmp, pass);
+    double gxd[3];
+    for (int k = 0; k < 3; ++k) {
+      gxd[k] = pass[k] ? g1[k] : 0.0;
+      g0[k] += gxd[k];
+    }
+    gvv[2] += gxd[1];
+    // xd0 = yd2 s, xd2 = -yd0 s
+    double gs = gxd[0] * yd[2] - gxd[2] * yd[0];
+    const double gyd[3] = {-gxd[2] * s, 0.0, gxd[0] * s};
+    const double down[3] = {0, -1, 0};
+    qrot_vjp(p0 + 3, down, gyd, g0 + 3, nullptr);
+    gvv[0] += gs * 0.03;
+    if (tl.type == T_ROLLINGPINEXT) gvv[3] += gs;
+    const double wa[3] = {0, -vv[1], 0}, wb[3] = {0, vv[0], 0};
+    double qa[4], qb[4], t[4];
+    w2quat(wa, qa);
+    w2quat(wb, qb);
+    qmul(p0 + 3, qb, t);
+    double gqa[4] = {0, 0, 0, 0}, gt[4] = {0, 0, 0, 0}, gqb[4] = {0, 0, 0, 0};
+    qmul_vjp(qa, t, g1 + 3, gqa, gt);
+    qmul_vjp(p0 + 3, qb, gt, g0 + 3, gqb);
+    double gwa[3] = {0, 0, 0}, gwb[3] = {0, 0, 0};
+    w2quat_vjp(wa, gqa, gwa);
+    w2quat_vjp(wb, gqb, gwb);
+    gvv[1] -= gwa[1];
+    gvv[0] += gwb[1];
+    g0[7] += g1[7];
+    return;
+  }
+  clamp_xyz(tl, p0, vv, tmp, pass);
+  for (int k = 0; k < 3; ++k)
+    if (pass[k]) {
+      g0[k] += g1[k];
+      gvv[k] += g1[k];
+    }
+  double wq[4], gwq[4] = {0, 0, 0, 0};
+  w2quat(vv + 3, wq);
+  if (has_gap_vel(tl.type)) {
+    qmul_vjp(p0 + 3, wq, g1 + 3, g0 + 3, gwq);
+    double a = p0[7] - vv[6];
+    double mx = (tl.min_gap < a) ? a : tl.min_gap;
+    bool ok = (tl.min_gap < a) && (tl.type == T_CHOPSTICKS || mx < tl.max_gap);
+    if (ok) {
+      g0[7] += g1[7];
+      gvv[6] -= g1[7];
+    }
+  } else {
+    qmul_vjp(wq, p0 + 3, g1 + 3, gwq, g0 + 3);
+    g0[7] += g1[7];
+  }
+  w2quat_vjp(vv + 3, gwq, gvv + 3);
+}
+// Box._project of rand * size, moved to the box pose (get_surface_pos, primive_base.py:285-287)
+inline void surface_pt(const OracleTool& box, const double* pose8, const double* rn, double* local, double* w) {
+  for (int k = 0; k < 3; ++k) local[k] = std::max(std::min(rn[k] * box.size[k], box.size[k]), -box.size[k]);
+  qrot(pose8 + 3, local, w);
+  for (int k = 0; k < 3; ++k) w[k] += pose8[k];
+}
+void project(const OracleTool* tools, int T, const std::vector<Pair>& pr, const double* pts, double* pose1,
+             double* coll) {
+  for (size_t c = 0; c < pr.size(); ++c) {  // set_surface_points + set_collision_idx
+    const Pair& P = pr[c];
+    double min_dist = 0.0;
+    int idx = -1;
+    double best[3] = {0, 0, 0};
+    for (int k = 0; k < kSurfacePoints; ++k) {
+      double local[3], w[3];
+      surface_pt(tools[P.j], pose1 + 8 * P.j, pts + 3 * (c * kSurfacePoints + k), local, w);
+      double d = tool_sdf(tools[P.i], pose1 + 8 * P.i, w);
+      if (d < min_dist) {
+        min_dist = d;
+        idx = k;
+        std::memcpy(best, w, sizeof(best));
+      }
+    }
+    coll[4 * c] = idx;
+    coll[4 * c + 1] = best[0];
+    coll[4 * c + 2] = best[1];
+    coll[4 * c + 3] = best[2];
+  }
+  for (size_t c = 0; c < pr.size(); ++c) {  // apply_collision_projection
+    if (coll[4 * c] < 0) continue;
+    const Pair& P = pr[c];
+    const double* w = coll + 4 * c + 1;
+    double d = tool_sdf(tools[P.i], pose1 + 8 * P.i, w), n[3];
+    tool_normal(tools[P.i], pose1 + 8 * P.i, w, n);
+    double L = std::sqrt(dot3(n, n));
+    for (int k = 0; k < 3; ++k) pose1[8 * P.i + k] += n[k] / L * d;
+  }
+}
+// apply_collision_projection.grad + set_surface_points.grad at the stored
+// (projected) poses and stored points, pairs in reverse
+void project_vjp(const OracleTool* tools, int T, const std::vector<Pair>& pr, const double* pts, const double* pose1,
+                 const double* coll, double* g1) {
+  for (int c = (int)pr.size() - 1; c >= 0; --c) {
+    if (coll[4 * c] < 0) continue;
+    const Pair& P = pr[c];
+    const double* w = coll + 4 * c + 1;
+    const double* pi = pose1 + 8 * P.i;
+    double d = tool_sdf(tools[P.i], pi, w), n[3];
+    tool_normal(tools[P.i], pi, w, n);
+    double L = std::sqrt(dot3(n, n));
+    double nn[3] = {n[0] / L, n[1] / L, n[2] / L};
+    const double gs[3] = {g1[8 * P.i], g1[8 * P.i + 1], g1[8 * P.i + 2]};
+    double gd = dot3(gs, nn);
+    double gnn[3] = {gs[0] * d, gs[1] * d, gs[2] * d};
+    double dn = dot3(nn, gnn);
+    double gn[3];
+    for (int k = 0; k < 3; ++k) gn[k] = (gnn[k] - nn[k] * dn) / L;
+    double gp[3] = {0, 0, 0};
+    tool_sdf_vjp(tools[P.i], pi, w, gd, gp, g1 + 8 * P.i);
+    tool_normal_vjp(tools[P.i], pi, w, gn, gp, g1 + 8 * P.i);
+    double local[3], ww[3];
+    surface_pt(tools[P.j], pose1 + 8 * P.j, pts + 3 * (c * kSurfacePoints + (int)coll[4 * c]), local, ww);
+    for (int k = 0; k < 3; ++k) g1[8 * P.j + k] += gp[k];
+    qrot_vjp(pose1 + 8 * P.j + 3, local, gp, g1 + 8 * P.j + 3, nullptr);
+  }
+}
+}  // namespace
+extern "C" {
+int oracle_collision_pairs(const OracleTool* tools, int T) { return (int)collision_pairs(tools, T).size(); }
+void oracle_tools_action(const OracleTool* tools, int T, int n_sub, const double* action, double* vel, double* pose,
+                         const double* pts, double* coll) {
+  const std::vector<Pair> pr = collision_pairs(tools, T);
+  const int np = (int)pr.size();
   for (int t = 0; t < T; ++t) {
     const OracleTool& tl = tools[t];
     double vv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -1223,33 +1612,15 @@ void oracle_tools_action(const OracleTool* tools, int T, int n_sub, const double
       for (int k = 0; k < 3; ++k) vv[k] = action[t * 7 + k] * tl.action_scale[k] / n_sub;
       if (tl.action_dim > 3)
         for (int k = 0; k < 3; ++k) vv[3 + k] = action[t * 7 + 3 + k] * tl.action_scale[3 + k] / n_sub;
-      if (tl.type == T_GRIPPER) vv[6] = action[t * 7 + 6] * tl.action_scale[6] / n_sub;
+      if (has_gap_vel(tl.type)) vv[6] = action[t * 7 + 6] * tl.action_scale[6] / n_sub;
     }
     for (int j = 0; j < n_sub; ++j) std::memcpy(vel + ((int64_t)j * T + t) * 8, vv, sizeof(vv));
   }
   for (int j = 0; j < n_sub; ++j) {
-    for (int t = 0; t < T; ++t) {
-      const OracleTool& tl = tools[t];
-      const double* p0 = pose + ((int64_t)j * T + t) * 8;
-      double* p1 = pose + ((int64_t)(j + 1) * T + t) * 8;
-      const double* vv = vel + ((int64_t)j * T + t) * 8;
-      for (int k = 0; k < 3; ++k) {
-        double a = p0[k] + vv[k];
-        double mn = (a < tl.upper[k]) ? a : tl.upper[k];
-        p1[k] = (tl.lower[k] < mn) ? mn : tl.lower[k];
-      }
-      double wq[4];
-      w2quat(vv + 3, wq);
-      if (tl.type == T_GRIPPER) {
-        qmul(p0 + 3, wq, p1 + 3);
-        double a = p0[7] - vv[6];
-        double mx = (tl.min_gap < a) ? a : tl.min_gap;
-        p1[7] = (mx < tl.max_gap) ? mx : tl.max_gap;
-      } else {
-        qmul(wq, p0 + 3, p1 + 3);
-        p1[7] = p0[7];
-      }
-    }
+    for (int t = 0; t < T; ++t)
+      fk(tools[t], pose + ((int64_t)j * T + t) * 8, vel + ((int64_t)j * T + t) * 8,
+         pose + ((int64_t)(j + 1) * T + t) * 8);
+    if (np) project(tools, T, pr, pts, pose + (int64_t)(j + 1) * T * 8, coll + (int64_t)j * np * 4);
   }
 }
 // Adjoint of oracle_tools_action.  g_pose [(n_sub+1)][T][8] holds the
@@ -1258,47 +1629,25 @@ void oracle_tools_action(const OracleTool* tools, int T, int n_sub, const double
 // (set_velocity.grad, primive_base.py:260-268, without the clip mask, as
 // GradModel.backward returns it).
 void oracle_tools_action_bwd(const OracleTool* tools, int T, int n_sub, const double* action, const double* vel,
-                             const double* pose, double* g_pose, double* g_action) {
+                             const double* pose, const double* pts, const double* coll, double* g_pose,
+                             double* g_action) {
   (void)action;
+  const std::vector<Pair> pr = collision_pairs(tools, T);
+  const int np = (int)pr.size();
   for (int j = n_sub - 1; j >= 0; --j) {
+    if (np)
+      project_vjp(tools, T, pr, pts, pose + (int64_t)(j + 1) * T * 8, coll + (int64_t)j * np * 4,
+                  g_pose + (int64_t)(j + 1) * T * 8);
     for (int t = 0; t < T; ++t) {
       const OracleTool& tl = tools[t];
-      const double* p0 = pose + ((int64_t)j * T + t) * 8;
-      const double* vv = vel + ((int64_t)j * T + t) * 8;
-      double* g1 = g_pose + ((int64_t)(j + 1) * T + t) * 8;
-      double* g0 = g_pose + ((int64_t)j * T + t) * 8;
       double gvv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      for (int k = 0; k < 3; ++k) {
-        double a = p0[k] + vv[k];
-        double mn = (a < tl.upper[k]) ? a : tl.upper[k];
-        bool pass = (a < tl.upper[k]) && (tl.lower[k] < mn);
-        if (pass) {
-          g0[k] += g1[k];
-          gvv[k] += g1[k];
-        }
-      }
-      double wq[4];
-      w2quat(vv + 3, wq);
-      double gwq[4] = {0, 0, 0, 0};
-      if (tl.type == T_GRIPPER) {
-        qmul_vjp(p0 + 3, wq, g1 + 3, g0 + 3, gwq);
-        double a = p0[7] - vv[6];
-        double mx = (tl.min_gap < a) ? a : tl.min_gap;
-        bool pass = (tl.min_gap < a) && (mx < tl.max_gap);
-        if (pass) {
-          g0[7] += g1[7];
-          gvv[6] -= g1[7];
-        }
-      } else {
-        qmul_vjp(wq, p0 + 3, g1 + 3, gwq, g0 + 3);
-        g0[7] += g1[7];
-      }
-      w2quat_vjp(vv + 3, gwq, gvv + 3);
+      fk_vjp(tl, pose + ((int64_t)j * T + t) * 8, vel + ((int64_t)j * T + t) * 8,
+             g_pose + ((int64_t)(j + 1) * T + t) * 8, g_pose + ((int64_t)j * T + t) * 8, gvv);
       if (tl.action_dim > 0) {
         for (int k = 0; k < 3; ++k) g_action[t * 7 + k] += gvv[k] * tl.action_scale[k] / n_sub;
         if (tl.action_dim > 3)
           for (int k = 0; k < 3; ++k) g_action[t * 7 + 3 + k] += gvv[3 + k] * tl.action_scale[3 + k] / n_sub;
-        if (tl.type == T_GRIPPER) g_action[t * 7 + 6] += gvv[6] * tl.action_scale[6] / n_sub;
+        if (has_gap_vel(tl.type)) g_action[t * 7 + 6] += gvv[6] * tl.action_scale[6] / n_sub;
       }
     }
   }

@@ -49,7 +49,8 @@ class OracleToolStruct(ctypes.Structure):
                 ("size", ctypes.c_double * 3), ("prism_h", ctypes.c_double * 2), ("prot", ctypes.c_double * 4),
                 ("min_gap", ctypes.c_double), ("max_gap", ctypes.c_double),
                 ("lower", ctypes.c_double * 3), ("upper", ctypes.c_double * 3),
-                ("action_scale", ctypes.c_double * 7)]
+                ("action_scale", ctypes.c_double * 7), ("torus", ctypes.c_double * 2),
+                ("collision_mask", ctypes.c_int32), ("pad1", ctypes.c_int32)]
 
 
 def build(force: bool = False, quiet: bool = True) -> str:
@@ -82,6 +83,7 @@ def lib():
         L.oracle_contact_min.restype = ctypes.c_double
         L.oracle_contact_min.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int64, _dp, ctypes.c_double, _dp, _dp,
                                          ctypes.POINTER(ctypes.c_int64)]
+        L.oracle_collision_pairs.restype = ctypes.c_int
         L.oracle_target_sdf_f64.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp, _dp, _dp]
         _fp = ctypes.POINTER(ctypes.c_float)
         L.oracle_target_sdf_f32.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, _fp, _fp, _fp]
@@ -129,7 +131,15 @@ def tool_struct(t, softness: float) -> OracleToolStruct:
     s.lower[:] = list(t.lower_bound)
     s.upper[:] = list(t.upper_bound)
     s.action_scale[:] = list(t.scale7())
+    s.torus[:] = [t.tx, t.ty]
+    s.collision_mask = t.collision_mask
     return s
+
+
+def collision_points(n_pairs: int) -> np.ndarray:
+    """rand_num of the collision projection (mpm_simulator.py:89-96):
+    np.random.seed(42); uniform(-1.5, 1.5, (n_pairs, 600, 3))."""
+    return np.ascontiguousarray(np.random.RandomState(42).uniform(-1.5, 1.5, (max(n_pairs, 1), 600, 3)))
 
 
 def init_state(x0: np.ndarray) -> np.ndarray:
@@ -192,6 +202,8 @@ class Oracle:
         for t in self.tool_cfgs:
             self.dims.append(self.dims[-1] + int(t.action.dim))
         self.G = sim.grid ** 3
+        self.n_pairs = int(lib().oracle_collision_pairs(self.tools, self.T))
+        self.pts = collision_points(self.n_pairs)
 
     # -- tools ---------------------------------------------------------------
     def pose0(self) -> np.ndarray:
@@ -210,8 +222,16 @@ class Oracle:
         vel = np.zeros((self.n_sub, self.T, 8))
         poses = np.zeros((self.n_sub + 1, self.T, 8))
         poses[0] = pose_start
-        lib().oracle_tools_action(self.tools, self.T, self.n_sub, ptr(act), ptr(vel), ptr(poses))
+        coll = np.zeros((self.n_sub, max(self.n_pairs, 1), 4))
+        lib().oracle_tools_action(self.tools, self.T, self.n_sub, ptr(act), ptr(vel), ptr(poses), ptr(self.pts),
+                                  ptr(coll))
+        self.last_coll = coll  # collision records of this action, for tools_action_bwd
         return act, vel, poses
+
+    def tools_action_bwd(self, act, vel, pseq, coll, g_pose_seq, g_act) -> None:
+        """Adjoint of one action's kinematics: g_pose_seq [(n_sub+1)][T][8] in/out, g_act [T][7] accumulated."""
+        lib().oracle_tools_action_bwd(self.tools, self.T, self.n_sub, ptr(act), ptr(vel), ptr(np.ascontiguousarray(pseq)),
+                                      ptr(self.pts), ptr(coll), ptr(g_pose_seq), ptr(g_act))
 
     # -- substep -------------------------------------------------------------
     def substep(self, pose_f, pose_f1, state) -> np.ndarray:
@@ -258,11 +278,12 @@ class Oracle:
         frames: List[np.ndarray] = [state]
         pose = self.pose0()
         poses = [pose[None]]
-        vels, acts = [], []
+        vels, acts, colls = [], [], []
         for a in actions:
             act, vel, pseq = self.tools_action(pose, a)
             acts.append(act)
             vels.append(vel)
+            colls.append(self.last_coll)
             for j in range(self.n_sub):
                 state = self.substep(pseq[j], pseq[j + 1], state)
                 if keep_frames:
@@ -271,7 +292,7 @@ class Oracle:
             poses.append(pseq[1:])
         if not keep_frames:
             frames = [frames[0], state]
-        return dict(frames=frames, poses=np.concatenate(poses), vels=vels, acts=acts, final=state)
+        return dict(frames=frames, poses=np.concatenate(poses), vels=vels, acts=acts, colls=colls, final=state)
 
     def loss(self, final_state, target, poses_last=None, density_weight=1.0, contact_weight=0.0) -> float:
         gm = self.grid_mass(final_state)
@@ -311,8 +332,7 @@ class Oracle:
             sl = g_pose[s * self.n_sub:(s + 1) * self.n_sub + 1]
             assert sl.flags["C_CONTIGUOUS"]
             pseq = np.ascontiguousarray(poses[s * self.n_sub:(s + 1) * self.n_sub + 1])
-            lib().oracle_tools_action_bwd(self.tools, self.T, self.n_sub, ptr(ro["acts"][s]), ptr(ro["vels"][s]),
-                                          ptr(pseq), ptr(sl), ptr(g_act[s]))
+            self.tools_action_bwd(ro["acts"][s], ro["vels"][s], pseq, ro["colls"][s], sl, g_act[s])
         flat = np.zeros((A, self.dims[-1]))
         for i in range(self.T):
             d = self.dims[i + 1] - self.dims[i]

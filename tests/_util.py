@@ -61,3 +61,42 @@ def small_scene(n: int = 2000, n_actions: int = 1, substeps: int = 10, tools=Non
         dims = sum(int(t.action.dim) for t in sc.tools)
         sc.actions = rng.uniform(-1, 1, size=(n_actions, dims))
     return sc
+
+
+def more_tools():
+    """One tool of each remaining shape (RollingPin, RollingPinExt, Chopsticks,
+    Cylinder, Torus, Gripper2), placed to touch the dough of ``small_scene``."""
+    rot6 = ActionConfig(dim=6, scale=(0.02, 0.02, 0.02, 0.05, 0.05, 0.05))
+    return [
+        PrimitiveConfig(shape="RollingPin", init_pos=(0.45, 0.22, 0.5), init_rot=(0.707, 0.707, 0.0, 0.0), h=0.2,
+                        r=0.03, action=ActionConfig(dim=3, scale=(0.7, 0.02, 0.01))),
+        PrimitiveConfig(shape="RollingPinExt", init_pos=(0.55, 0.22, 0.5), init_rot=(0.707, 0.707, 0.0, 0.0),
+                        h=0.2, r=0.03, action=ActionConfig(dim=6, scale=(0.7, 0.02, 0.01, 0.01, 0.0, 0.0))),
+        PrimitiveConfig(shape="Chopsticks", init_pos=(0.45, 0.25, 0.48), init_rot=(0.9, 0.1, 0.3, 0.2), h=0.12,
+                        r=0.015, init_gap=0.07, minimal_gap=0.03,
+                        action=ActionConfig(dim=7, scale=(0.02, 0.02, 0.02, 0.05, 0.05, 0.05, 0.02))),
+        PrimitiveConfig(shape="Cylinder", init_pos=(0.56, 0.215, 0.45), init_rot=(0.9, 0.1, 0.3, 0.2), h=0.04,
+                        r=0.02, action=rot6),
+        PrimitiveConfig(shape="Torus", init_pos=(0.5, 0.21, 0.56), init_rot=(0.9, 0.1, 0.3, 0.2), tx=0.04, ty=0.015,
+                        action=rot6),
+        PrimitiveConfig(shape="Gripper2", init_pos=(0.5, 0.17, 0.5), init_rot=(0.9, 0.1, 0.3, 0.2), h=0.06, r=0.015,
+                        init_gap=0.1, minimal_gap=0.04, maximal_gap=0.3, friction=2.0,
+                        action=ActionConfig(dim=7, scale=(0.02, 0.02, 0.02, 0.05, 0.05, 0.05, 0.02))),
+    ]
+
+
+def collision_tools():
+    """A gripper and a lifter box projected out of a static obstacle box
+    (collision_group (0, 0, 1) as in plb/envs/gather_move.yml), overlapping it
+    at the start so that the projection acts."""
+    return [
+        PrimitiveConfig(shape="Gripper", init_pos=(0.5, 0.215, 0.5), size=(0.01, 0.04, 0.04), init_gap=0.12,
+                        minimal_gap=0.04, maximal_gap=0.3, friction=2.0, init_rot=(1.0, 0.0, 0.0, 0.0),
+                        collision_group=(0, 0, 1),
+                        action=ActionConfig(dim=7, scale=(0.02, 0.03, 0.02, 0.0, 0.05, 0.0, 0.02))),
+        PrimitiveConfig(shape="Box", init_pos=(0.42, 0.21, 0.42), size=(0.03, 0.01, 0.03), friction=5.0,
+                        collision_group=(0, 0, 1),
+                        action=ActionConfig(dim=6, scale=(0.02, 0.03, 0.02, 0.0, 0.05, 0.0))),
+        PrimitiveConfig(shape="Box", init_pos=(0.5, 0.16, 0.5), size=(0.12, 0.04, 0.12), friction=5.0,
+                        action=ActionConfig(dim=0)),
+    ]

@@ -50,9 +50,7 @@ def oracle_obs_grad(o, x0, actions, Wx, Wc, Wd=None):
     g_act = np.zeros((A, o.T, 7))
     for s in range(A - 1, -1, -1):
         sl = gp[s * n:(s + 1) * n + 1]
-        O.lib().oracle_tools_action_bwd(o.tools, o.T, n, O.ptr(ro["acts"][s]), O.ptr(ro["vels"][s]),
-                                        O.ptr(np.ascontiguousarray(poses[s * n:(s + 1) * n + 1])), O.ptr(sl),
-                                        O.ptr(g_act[s]))
+        o.tools_action_bwd(ro["acts"][s], ro["vels"][s], poses[s * n:(s + 1) * n + 1], ro["colls"][s], sl, g_act[s])
     flat = np.concatenate([g_act[:, i, :o.dims[i + 1] - o.dims[i]] for i in range(o.T)], axis=1)
     return loss, flat
 

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 import torch
 
-from _util import all_tools, group_errors, perturbed_state, rel_err, small_scene
+from _util import all_tools, collision_tools, group_errors, more_tools, perturbed_state, rel_err, small_scene
 from diffskill_gb300.config import PrimitiveConfig
 from diffskill_gb300.engine import Horizon, MpmEngine
 from oracle.oracle import Oracle, init_state
@@ -109,8 +109,7 @@ def test_tools_action_matches_oracle(gpu_lib):
     from oracle.oracle import lib, ptr
     gps = np.random.default_rng(1).normal(size=pseq.shape)
     g_ref, ga_ref = gps.copy(), np.zeros((o.T, 7))
-    lib().oracle_tools_action_bwd(o.tools, o.T, n, ptr(acts), ptr(vel), ptr(np.ascontiguousarray(pseq)), ptr(g_ref),
-                                  ptr(ga_ref))
+    o.tools_action_bwd(acts, vel, pseq, o.last_coll, g_ref, ga_ref)
     g = torch.as_tensor(gps, device=eng.device).contiguous()
     ga = torch.zeros((o.T, 8), dtype=torch.float64, device=eng.device)
     eng.tools_action_bwd(v, p, g, ga)
@@ -337,3 +336,95 @@ def test_resorting_particles_keeps_loss_and_gradients(gpu_lib, k):
     assert rel_err(g1, g0) < 1e-9
     # the gradient w.r.t. the initial state comes back in the original particle order
     assert rel_err(s1.cpu().numpy(), s0.cpu().numpy()) < 1e-9
+
+
+
+# ----------------------------------------------------------------------------
+# RollingPin(Ext), Chopsticks, Cylinder, Torus, Gripper2 and the tool-tool
+# collision projection
+# ----------------------------------------------------------------------------
+@pytest.mark.parametrize("prec,fwd_tol,bwd_tol", [("fp64", 1e-9, 1e-8), ("fp32", 1e-4, 2e-3)])
+def test_more_tools_substep_matches_oracle(gpu_lib, prec, fwd_tol, bwd_tol):
+    tools = more_tools()
+    sc = small_scene(n=3000, tools=tools, precision=prec)
+    eng = make_engine(sc)
+    o = Oracle(sc.sim, tools)
+    st0 = perturbed_state(sc.x0, seed=13)
+    _, _, pseq = o.tools_action(o.pose0(), sc.actions[0])
+    pose = torch.as_tensor(pseq[:2], device=eng.device).contiguous()
+    ref = o.substep(pseq[0], pseq[1], st0)
+    s0, s1 = to_soa(eng, st0), eng.new_state()
+    eng.substep(s0, s1, pose[0], pose[1])
+    torch.cuda.synchronize()
+    assert eng.status() == 0
+    errs = group_errors(to_aos(eng, s1), ref)
+    assert max(errs.values()) < fwd_tol, errs
+    g1 = np.random.default_rng(14).normal(size=st0.shape)
+    gp_f, gp_f1 = np.zeros((o.T, 8)), np.zeros((o.T, 8))
+    gref = o.substep_bwd(pseq[0], pseq[1], st0, g1, gp_f, gp_f1)
+    gpose = torch.zeros((2, o.T, 8), dtype=torch.float64, device=eng.device)
+    gg0 = eng.new_state()
+    eng.substep_bwd(s0, to_soa(eng, g1), gg0, pose[0], pose[1], gpose[0], gpose[1])
+    torch.cuda.synchronize()
+    errs = group_errors(to_aos(eng, gg0), gref)
+    assert max(errs.values()) < bwd_tol, errs
+    gp = gpose.cpu().numpy()
+    assert np.abs(gp_f).max() > 0 and np.abs(gp_f1).max() > 0  # every tool touches the dough
+    assert rel_err(gp[0], gp_f) < bwd_tol * 10 and rel_err(gp[1], gp_f1) < bwd_tol * 10
+
+
+@pytest.mark.parametrize("which", ["more", "collision"])
+def test_kinematics_and_collision_projection_match_oracle(gpu_lib, which):
+    """mpm_tools_action(_bwd) for the remaining tools' kinematics and for tools
+    projected out of an obstacle box (oracle: the reference's sequential
+    set_collision_idx loop and its autodiff semantics)."""
+    tools = more_tools() if which == "more" else collision_tools()
+    sc = small_scene(n=100, tools=tools, precision="fp64", substeps=20, n_actions=2)
+    eng = make_engine(sc)
+    o = Oracle(sc.sim, tools)
+    assert eng.n_pairs == o.n_pairs == (2 if which == "collision" else 0)
+    n = sc.sim.n_substeps
+    pose_o = o.pose0()
+    p0 = eng.pose0.clone()
+    for s in range(sc.n_actions):
+        acts, vel, pseq = o.tools_action(pose_o, sc.actions[s])
+        a = torch.zeros((o.T, 8), dtype=torch.float64, device=eng.device)
+        a[:, :7] = torch.as_tensor(acts, device=eng.device)
+        v = torch.zeros((n, o.T, 8), dtype=torch.float64, device=eng.device)
+        p = torch.zeros((n + 1, o.T, 8), dtype=torch.float64, device=eng.device)
+        p[0] = p0
+        coll = eng.new_coll(1)
+        eng.tools_action(a, v, p, None if coll is None else coll[0])
+        torch.cuda.synchronize()
+        assert rel_err(p.cpu().numpy(), pseq) < 1e-12, s
+        if which == "collision":
+            c = coll[0].cpu().numpy()
+            assert (c[..., 0] >= 0).any()
+            assert np.array_equal(c[..., 0] >= 0, o.last_coll[..., 0] >= 0)
+        gps = np.random.default_rng(s).normal(size=pseq.shape)
+        g_ref, ga_ref = gps.copy(), np.zeros((o.T, 7))
+        o.tools_action_bwd(acts, vel, pseq, o.last_coll, g_ref, ga_ref)
+        g = torch.as_tensor(gps, device=eng.device).contiguous()
+        ga = torch.zeros((o.T, 8), dtype=torch.float64, device=eng.device)
+        eng.tools_action_bwd(v, p, g, ga, None if coll is None else coll[0])
+        torch.cuda.synchronize()
+        assert rel_err(g.cpu().numpy(), g_ref) < 1e-10, s
+        assert rel_err(ga.cpu().numpy()[:, :7], ga_ref) < 1e-10, s
+        pose_o, p0 = pseq[-1], p[-1].clone()
+
+
+def test_collision_trajectory_loss_and_grad(gpu_lib):
+    """Horizon over actions with tool-tool projections against the oracle's
+    store-all rollout and reverse sweep."""
+    tools = collision_tools()
+    sc = small_scene(n=3000, tools=tools, precision="fp64", substeps=10, n_actions=2)
+    eng = make_engine(sc)
+    o = Oracle(sc.sim, tools)
+    loss_ref, grad_ref = o.loss_and_grad(sc.x0, sc.actions, sc.target)
+    hz = Horizon(eng, sc.n_actions, ckpt_every=5)
+    hz.forward(eng.init_state([sc.x0]), eng.expand_actions([sc.actions]))
+    loss = float(hz.loss(eng.targets([sc.target])).sum())
+    g = eng.collapse_action_grad(hz.backward())[0].cpu().numpy()
+    torch.cuda.synchronize()
+    assert abs(loss - loss_ref) < 1e-12 * abs(loss_ref)
+    assert rel_err(g, grad_ref) < 1e-8

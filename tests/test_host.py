@@ -34,7 +34,17 @@ def test_primitive_config_and_action_dims():
     assert C.action_dims([b, g, b]) == [0, 3, 10, 13]
     assert b.scale7() == (0.5, 0.5, 0.5, 0.0, 0.0, 0.0, 0.0)
     with pytest.raises(ValueError):
-        C.make_primitive("Torus").type_code
+        C.make_primitive("Teapot").type_code
+    # the remaining primitives of primitives.py
+    codes = {n: C.make_primitive(n).type_code for n in ("RollingPin", "RollingPinExt", "Chopsticks", "Cylinder",
+                                                        "Torus", "Gripper2")}
+    assert sorted(codes.values()) == list(range(5, 11))
+    assert C.make_primitive("Chopsticks").state_dim == 8 and C.make_primitive("Gripper2").state_dim == 8
+    assert C.make_primitive("Torus").state_dim == 7
+    cyl = C.make_primitive("Cylinder")
+    assert (cyl.h, cyl.r) == (0.2, 0.1) and C.make_primitive("Gripper2").r == 0.015
+    assert C.make_primitive("Box", collision_group=(0, 0, 1)).collision_mask == 4
+    assert C.make_primitive("Box", collision_group=(1., 0, 1)).collision_mask == 5
 
 
 def test_workloads_are_seeded_and_in_bounds():

@@ -6,7 +6,7 @@ import os
 import numpy as np
 import pytest
 
-from _util import all_tools, perturbed_state, small_scene
+from _util import all_tools, collision_tools, more_tools, perturbed_state, small_scene
 from diffskill_gb300 import scenes
 from oracle import oracle as O
 
@@ -228,8 +228,7 @@ def test_tools_action_adjoint_matches_finite_differences():
     acts, vel, pseq = o.tools_action(o.pose0(), a)
     gp = W.copy()
     ga = np.zeros((o.T, 7))
-    O.lib().oracle_tools_action_bwd(o.tools, o.T, sc.sim.n_substeps, O.ptr(acts), O.ptr(vel),
-                                    O.ptr(np.ascontiguousarray(pseq)), O.ptr(gp), O.ptr(ga))
+    o.tools_action_bwd(acts, vel, pseq, o.last_coll, gp, ga)
     flat = np.concatenate([ga[i, :o.dims[i + 1] - o.dims[i]] for i in range(o.T)])
     for k in range(len(a)):
         fds = _fd_best(f, a, k, (1e-5, 1e-6))
@@ -392,3 +391,176 @@ def test_contact_min_and_its_adjoint():
             e[am, d] = 1e-7
             fd = (o.contact_min(t, pose[t], st + e)[0] - o.contact_min(t, pose[t], st - e)[0]) / 2e-7
             assert abs(fd - g[am, d]) < 1e-5
+
+
+# --------------------------------------------------------------------------
+# the remaining tools of primitives.py and the tool-tool collision projection
+# --------------------------------------------------------------------------
+@pytest.mark.parametrize("ti", range(6))
+def test_more_tools_normal_matches_sdf_gradient(ti):
+    """test_primitives.py:34-67's property for RollingPin(Ext), Chopsticks,
+    Cylinder, Torus and Gripper2: the analytic normal is the normalised SDF
+    gradient away from the shapes' kinks."""
+    tool = more_tools()[ti]
+    ts = O.tool_struct(tool, 666.0)
+    pose = np.array(tool.init_state, dtype=np.float64)
+    pose[3:7] /= np.linalg.norm(pose[3:7])
+    rng = np.random.default_rng(40 + ti)
+    pts = pose[:3] + rng.normal(size=(400, 3)) * 0.05
+    sdf, nrm = np.zeros(400), np.zeros((400, 3))
+    O.lib().oracle_tool_sdf(ctypes_ref(ts), O.ptr(pose), 400, O.ptr(pts), O.ptr(sdf), O.ptr(nrm))
+    fd = np.zeros((400, 3))
+    for k in range(3):
+        e = np.zeros(3)
+        e[k] = 1e-7
+        sp, sm = np.zeros(400), np.zeros(400)
+        O.lib().oracle_tool_sdf(ctypes_ref(ts), O.ptr(pose), 400, O.ptr(pts + e), O.ptr(sp), None)
+        O.lib().oracle_tool_sdf(ctypes_ref(ts), O.ptr(pose), 400, O.ptr(pts - e), O.ptr(sm), None)
+        fd[:, k] = (sp - sm) / 2e-7
+    fdn = fd / np.linalg.norm(fd, axis=1, keepdims=True)
+    err = np.linalg.norm(fdn - nrm, axis=1)
+    assert np.median(err) < 1e-5 and np.mean(err < 1e-4) > 0.9, (tool.shape, np.median(err))
+
+
+@pytest.mark.parametrize("ti", range(6))
+def test_more_tools_substep_adjoint_matches_finite_differences(ti):
+    tools = [more_tools()[ti]]
+    sc = small_scene(n=250, substeps=3, tools=tools, precision="fp64")
+    sc.sim.yield_stress = 5.0
+    o = O.Oracle(sc.sim, tools)
+    st0 = perturbed_state(sc.x0, seed=ti)
+    rng = np.random.default_rng(200 + ti)
+    W = rng.normal(size=st0.shape)
+    a = sc.actions[0]
+    K = sc.sim.n_substeps
+
+    def run(st, frames=None):
+        _, _, pseq = o.tools_action(o.pose0(), a)
+        s = st
+        for j in range(K):
+            if frames is not None:
+                frames.append(s)
+            s = o.substep(pseq[j], pseq[j + 1], s)
+        return float((W * s).sum()), pseq
+
+    frames = []
+    _, pseq = run(st0, frames)
+    g = W.copy()
+    gp = np.zeros((K + 1, o.T, 8))
+    for f in range(K - 1, -1, -1):
+        g = o.substep_bwd(pseq[f], pseq[f + 1], frames[f], g, gp[f], gp[f + 1])
+    for i in [int(i) for i in rng.integers(0, st0.size, size=12)]:
+        fds = _fd_best(lambda s: run(s)[0], st0, i)
+        best = min(abs(v - g.flat[i]) / max(abs(v), 1e-8) for v in fds)
+        assert best < 1e-5, (i, g.flat[i], fds)
+    # the tool-pose gradients of the substeps (incl. the Chopsticks gap) through the kinematics
+    acts, vel, _ = o.tools_action(o.pose0(), a)
+    ga = np.zeros((o.T, 7))
+    o.tools_action_bwd(acts, vel, pseq, o.last_coll, gp, ga)
+    flat = ga[0, :int(tools[0].action.dim)]
+
+    def loss_of(act):
+        _, _, ps = o.tools_action(o.pose0(), act)
+        s = st0
+        for j in range(K):
+            s = o.substep(ps[j], ps[j + 1], s)
+        return float((W * s).sum())
+
+    for k in range(len(a)):
+        fds = _fd_best(loss_of, a, k, (1e-4, 1e-5, 1e-6))
+        best = min(abs(v - flat[k]) / max(abs(v), 1e-7) for v in fds)
+        assert best < 1e-4, (tools[0].shape, k, flat[k], fds)
+
+
+def test_more_tools_kinematics_adjoint_matches_finite_differences():
+    tools = more_tools()
+    sc = small_scene(n=10, substeps=7, tools=tools, precision="fp64")
+    o = O.Oracle(sc.sim, tools)
+    a = sc.actions[0]
+    rng = np.random.default_rng(5)
+    W = rng.normal(size=(sc.sim.n_substeps + 1, o.T, 8))
+
+    def f(act):
+        return float((W * o.tools_action(o.pose0(), act)[2]).sum())
+
+    acts, vel, pseq = o.tools_action(o.pose0(), a)
+    gp = W.copy()
+    ga = np.zeros((o.T, 7))
+    o.tools_action_bwd(acts, vel, pseq, o.last_coll, gp, ga)
+    flat = np.concatenate([ga[i, :o.dims[i + 1] - o.dims[i]] for i in range(o.T)])
+    for k in range(len(a)):
+        fds = _fd_best(f, a, k, (1e-5, 1e-6))
+        best = min(abs(v - flat[k]) / max(abs(v), 1e-8) for v in fds)
+        assert best < 1e-6, (k, flat[k], fds)
+    # RollingPin: rot' = w2quat((0,-dth,0)) rot w2quat((0,dw,0)) keeps the pin horizontal
+    rp = pseq[-1, 0]
+    axis = np.array([0.0, 1.0, 0.0])  # the capsule's local axis
+    q = rp[3:7] / np.linalg.norm(rp[3:7])
+    w, v = q[0], q[1:]
+    world_axis = axis + 2 * (w * np.cross(v, axis) + np.cross(v, np.cross(v, axis)))
+    assert abs(world_axis[1]) < 1e-9
+
+
+def test_collision_projection_picks_first_most_negative_point():
+    """set_collision_idx semantics: the first of the 600 surface points with the
+    smallest SDF below 0, and after the projection that point lies on the tool
+    surface (box against box)."""
+    tools = collision_tools()
+    sc = small_scene(n=10, substeps=5, tools=tools, precision="fp64")
+    o = O.Oracle(sc.sim, tools)
+    assert o.n_pairs == 2
+    acts, vel, pseq = o.tools_action(o.pose0(), sc.actions[0])
+    coll = o.last_coll
+    assert (coll[:, :, 0] >= 0).any()
+    for j in range(sc.sim.n_substeps):
+        # recompute the argmin of step j from the pre-projection poses: FK only
+        pre = pseq[j + 1].copy()
+        for c, (i, jj) in enumerate([(0, 2), (1, 2)]):
+            box = tools[jj]
+            rn = o.pts[c]
+            local = np.clip(rn * np.array(box.size), -np.array(box.size), np.array(box.size))
+            q = pre[jj, 3:7]
+            w_, v_ = q[0], q[1:]
+            world = local + 2 * (w_ * np.cross(v_, local) + np.cross(v_, np.cross(v_, local))) + pre[jj, :3]
+            if coll[j, c, 0] >= 0:
+                k = int(coll[j, c, 0])
+                assert np.allclose(world[k], coll[j, c, 1:]), (j, c)
+                # after the projection the chosen point is on tool i's surface
+                sd = np.zeros(1)
+                O.lib().oracle_tool_sdf(ctypes_ref(o.tools[i]), O.ptr(pseq[j + 1, i].copy()), 1,
+                                        O.ptr(coll[j, c, 1:].copy()), O.ptr(sd), None)
+                assert abs(sd[0]) < 1e-6, (j, c, sd)
+
+
+def test_collision_projection_adjoint_matches_finite_differences():
+    """The kinematics adjoint with projections (evaluated, as the reference's
+    autodiff does, at the projected poses) against central differences.  For
+    translations and the gripper gap of box-shaped tools the normal is constant
+    on a face and that evaluation is exact; with rotations the SDF's lever arm
+    at the projected position differs from the pre-projection one, so the
+    rotation actions are switched off here (the GPU tests compare those with
+    the oracle's reference semantics instead)."""
+    tools = collision_tools()
+    for t in tools:
+        sc7 = list(t.action.scale) + [0.0] * (7 - len(t.action.scale))
+        sc7[3:6] = [0.0, 0.0, 0.0]
+        t.action.scale = tuple(sc7[:max(int(t.action.dim), 0)])
+    sc = small_scene(n=10, substeps=5, tools=tools, precision="fp64")
+    o = O.Oracle(sc.sim, tools)
+    a = sc.actions[0]
+    rng = np.random.default_rng(9)
+    W = rng.normal(size=(sc.sim.n_substeps + 1, o.T, 8))
+
+    def f(act):
+        return float((W * o.tools_action(o.pose0(), act)[2]).sum())
+
+    acts, vel, pseq = o.tools_action(o.pose0(), a)
+    assert (o.last_coll[:, :, 0] >= 0).any()
+    gp = W.copy()
+    ga = np.zeros((o.T, 7))
+    o.tools_action_bwd(acts, vel, pseq, o.last_coll, gp, ga)
+    flat = np.concatenate([ga[i, :o.dims[i + 1] - o.dims[i]] for i in range(o.T)])
+    for k in range(len(a)):
+        fds = _fd_best(f, a, k, (1e-6, 1e-7))
+        best = min(abs(v - flat[k]) / max(abs(v), 1e-6) for v in fds)
+        assert best < 1e-5, (k, flat[k], fds)
