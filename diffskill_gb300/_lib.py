@@ -16,6 +16,7 @@ ABI_VERSION = 2
 MPM_OK = 0
 STATUS_OUT_OF_GRID = 1
 STATUS_NONFINITE = 2
+STATUS_RENDER_BOX = 4
 
 _c_p = ctypes.c_void_p
 _i32 = ctypes.c_int32
@@ -41,6 +42,16 @@ class MpmToolDesc(ctypes.Structure):
                 ("size", _f64 * 3), ("prism_h", _f64 * 2), ("prot", _f64 * 4),
                 ("min_gap", _f64), ("max_gap", _f64), ("lower", _f64 * 3), ("upper", _f64 * 3),
                 ("action_scale", _f64 * 7), ("torus", _f64 * 2)]
+
+
+class MpmRenderVolume(ctypes.Structure):
+    _fields_ = [("res", _i32 * 3), ("bake_size", _i32), ("dx", _f64), ("packed", _c_p), ("sdf", _c_p),
+                ("sdf_copy", _c_p), ("color", _c_p), ("bbox", _c_p), ("kbox", _c_p)]
+
+
+class MpmRenderView(ctypes.Structure):
+    _fields_ = [("v2w", ctypes.c_float * 16), ("w2v", ctypes.c_float * 16), ("res", _i32 * 2),
+                ("bias", ctypes.c_float * 2), ("sdf_threshold", ctypes.c_float), ("show_particles", _i32)]
 
 
 class MpmGridStore(ctypes.Structure):
@@ -73,6 +84,9 @@ SIGNATURES = {
     "mpm_iou": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_contact_min_dist": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_contact_min_dist_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
+    "mpm_render_bake": (_i32, [_c_p, _c_p, _i32, _c_p, ctypes.POINTER(MpmRenderVolume), _c_p]),
+    "mpm_render_trace": (_i32, [_c_p, ctypes.POINTER(MpmRenderVolume), ctypes.POINTER(MpmRenderView), _i32, _c_p,
+                                _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_tool_distance_cols": (_i32, [_c_p]),
     "mpm_tool_distance": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_tool_distance_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),

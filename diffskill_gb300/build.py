@@ -17,7 +17,11 @@ CSRC = os.path.join(HERE, "csrc")
 REPO = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "libmpm_gb300.so")
 BUILD_DIR = os.path.join(HERE, "_build")
-SOURCES = ["mpm_capi.cu", "mpm_fwd.cu", "mpm_bwd.cu", "mpm_loss.cu", "mpm_kinematics.cu", "mpm_static.cu"]
+SOURCES = ["mpm_capi.cu", "mpm_fwd.cu", "mpm_bwd.cu", "mpm_loss.cu", "mpm_kinematics.cu", "mpm_render.cu",
+           "mpm_static.cu"]
+# per-file flags: the renderer rounds every FP32 operation on its own (no FMA
+# contraction), as its reference arithmetic does
+EXTRA = {"mpm_render.cu": ("-fmad=false",)}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -61,7 +65,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if not force and up_to_date():
         return LIB
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: compile_one(s, verbose=verbose), SOURCES))
+        objs = list(ex.map(lambda s: compile_one(s, EXTRA.get(s, ()), verbose=verbose), SOURCES))
     tmp = LIB + ".tmp"
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -617,6 +617,68 @@ int mpm_contact_min_dist_bwd(MpmHandle* h, const void* state, const double* pose
   return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_contact_min_dist_bwd");
 }
 
+static int check_volume(MpmHandle* h, const MpmRenderVolume* v, const char* what) {
+  if (!v) return fail(h, MPM_E_INVALID, std::string(what) + ": NULL volume");
+  for (int c = 0; c < 3; ++c)
+    if (v->res[c] < 2 || v->res[c] > 4096)
+      return fail(h, MPM_E_INVALID, std::string(what) + ": volume resolution must be in [2, 4096]");
+  if (v->bake_size < 0 || v->bake_size > 64 || !(v->dx > 0))
+    return fail(h, MPM_E_INVALID, std::string(what) + ": bad bake_size or dx");
+  MPM_TRY(check_aligned(h, v->packed, "vol->packed"));
+  MPM_TRY(check_aligned(h, v->sdf, "vol->sdf"));
+  MPM_TRY(check_aligned(h, v->sdf_copy, "vol->sdf_copy"));
+  MPM_TRY(check_aligned(h, v->color, "vol->color"));
+  MPM_TRY(check_aligned(h, v->bbox, "vol->bbox"));
+  return check_aligned(h, v->kbox, "vol->kbox");
+}
+
+int mpm_render_bake(MpmHandle* h, const void* state, int32_t scene, const uint32_t* colors,
+                    const MpmRenderVolume* vol, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_render_bake: NULL handle");
+  if (scene < 0 || scene >= h->p.n_scenes) return fail(h, MPM_E_INVALID, "mpm_render_bake: scene out of range");
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, state, "state"));
+  MPM_TRY(check_volume(h, vol, "mpm_render_bake"));
+  const int64_t p0 = h->offsets[scene], n = h->offsets[scene + 1] - p0;
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e = h->p.precision == MPM_PREC_FP64
+                      ? mpm::launch_render_bake<double>(L, (const double*)state, p0, n, colors, *vol)
+                      : mpm::launch_render_bake<float>(L, (const float*)state, p0, n, colors, *vol);
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_render_bake");
+}
+
+int mpm_render_trace(MpmHandle* h, const MpmRenderVolume* vol, const MpmRenderView* view, int32_t scene,
+                     const double* pose, const float* tool_color, float* depth, float* normal, float* color,
+                     float* image, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_render_trace: NULL handle");
+  if (scene < 0 || scene >= h->p.n_scenes) return fail(h, MPM_E_INVALID, "mpm_render_trace: scene out of range");
+  if (!view || view->res[0] < 1 || view->res[1] < 1 || view->res[0] > 16384 || view->res[1] > 16384)
+    return fail(h, MPM_E_INVALID, "mpm_render_trace: bad view");
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_volume(h, vol, "mpm_render_trace"));
+  int t0 = 0, nt = 0;
+  for (int i = 0; i < h->n_tools; ++i)
+    if (h->h_tools[i].scene == scene) {
+      if (nt == 0) t0 = i;
+      ++nt;
+    }
+  if (nt > 0) {
+    MPM_TRY(check_aligned(h, pose, "pose"));
+    MPM_TRY(check_aligned(h, tool_color, "tool_color"));
+  }
+  MPM_TRY(check_aligned(h, depth, "depth"));
+  MPM_TRY(check_aligned(h, normal, "normal"));
+  MPM_TRY(check_aligned(h, color, "color"));
+  MPM_TRY(check_aligned(h, image, "image", true));
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e = h->p.precision == MPM_PREC_FP64
+                      ? mpm::launch_render_trace<double>(L, *vol, *view, t0, nt, pose, tool_color, depth, normal,
+                                                         color, image)
+                      : mpm::launch_render_trace<float>(L, *vol, *view, t0, nt, pose, tool_color, depth, normal,
+                                                        color, image);
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_render_trace");
+}
+
 int mpm_tool_distance_cols(MpmHandle* h) { return h ? h->n_cols : 0; }
 
 int mpm_tool_distance(MpmHandle* h, const void* state, const double* pose, void* out, void* stream) {

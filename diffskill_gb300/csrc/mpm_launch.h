@@ -1,5 +1,5 @@
 // Internal launch interface between the C ABI (mpm_capi.cu) and the kernel
-// translation units (mpm_fwd.cu, mpm_bwd.cu, mpm_loss.cu, mpm_kinematics.cu).
+// translation units (mpm_fwd.cu, mpm_bwd.cu, mpm_loss.cu, mpm_kinematics.cu, mpm_render.cu).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -92,6 +92,14 @@ cudaError_t launch_tool_distance(const LaunchCtx& L, const int* col_off, int n_c
 template <typename T>
 cudaError_t launch_tool_distance_bwd(const LaunchCtx& L, const int* col_off, const T* st, const double* pose,
                                      const T* g_out, T* gst, double* g_pose);
+// particle-SDF renderer (mpm_render.cu)
+template <typename T>
+cudaError_t launch_render_bake(const LaunchCtx& L, const T* st, int64_t p0, int64_t n, const unsigned int* colors,
+                               const MpmRenderVolume& v);
+template <typename T>
+cudaError_t launch_render_trace(const LaunchCtx& L, const MpmRenderVolume& v, const MpmRenderView& view, int t0,
+                                int nt, const double* pose, const float* tool_color, float* depth, float* normal,
+                                float* color, float* image);
 // tool kinematics of one action with collision projection (mpm_kinematics.cu)
 cudaError_t launch_tools_action(const LaunchCtx& L, int n_tools, const int* pair_off, int n_pairs,
                                 const double* coll_pts, const double* action, double* vel, double* pose, double* coll,

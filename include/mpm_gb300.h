@@ -64,6 +64,7 @@ extern "C" {
 /* status bits (sticky; cleared by mpm_status with clear=1) */
 #define MPM_STATUS_OUT_OF_GRID 1u /* a particle stencil left the grid; it was skipped */
 #define MPM_STATUS_NONFINITE 2u   /* a NaN/Inf velocity or deformation was produced */
+#define MPM_STATUS_RENDER_BOX 4u  /* mpm_render_bake: the particles' box exceeds the render volume */
 
 /* Simulator constants: MPMSimulator.__init__ (mpm_simulator.py:8-67). */
 typedef struct MpmParams {
@@ -275,6 +276,52 @@ int mpm_tool_distance(MpmHandle* h, const void* state, const double* pose, void*
  * rows of g_state and g_pose (double[n_tools][8]) from g_out. */
 int mpm_tool_distance_bwd(MpmHandle* h, const void* state, const double* pose, const void* g_out, void* g_state,
                           double* g_pose, void* stream);
+
+/* Particle-SDF renderer (ParticleSDFRaster, taichi_three/tina/core/particle_sdf.py,
+ * driven by plb/env_modeling/tina_renderer.py), as compute kernels writing
+ * device buffers.  A volume (RENDERER.voxel_res / dx / bake_size of
+ * plb/config/default_config.py:43-49; all buffers caller-owned device memory): */
+typedef struct MpmRenderVolume {
+  int32_t res[3];              /* voxels per axis (default 168^3) */
+  int32_t bake_size;           /* splat radius in voxels (default 6) */
+  double dx;                   /* voxel size (default 1/150) */
+  unsigned long long* packed;  /* uint64[res] scratch: (quantised distance << 24) | rgb */
+  float* sdf;                  /* float[res] baked SDF, smoothed twice */
+  float* sdf_copy;             /* float[res] scratch */
+  float* color;                /* float[res][3] */
+  float* bbox;                 /* float[2][3]: lower and upper corner of the volume */
+  int32_t* kbox;               /* int32[6] scratch */
+} MpmRenderVolume;
+/* One view (host struct): tina Engine's matrices and pixel sample offset. */
+typedef struct MpmRenderView {
+  float v2w[16], w2v[16];  /* Engine.V2W / W2V, row-major (camera = inverse(proj @ view)) */
+  int32_t res[2];          /* image size (x, y); pixel (i, j) at i * res[1] + j */
+  float bias[2];           /* sample offset in the pixel (0.5, 0.5 without TAA jitter) */
+  float sdf_threshold;     /* RENDERER.sdf_threshold (default 0.37 * 0.56) */
+  int32_t show_particles;  /* visualize_shape */
+} MpmRenderView;
+
+/* initialize_particles_kernel + build_sdf_from_particles (particle_sdf.py:548-568,
+ * 237-265) for the particles of one scene: the volume's box from the
+ * particles, a splat of (min(51 |voxel - p|, 255) << 24 | colour) by 64-bit
+ * atomicMin over (-size-1 .. size]^3 voxels around each particle, the decode
+ * into SDF / colour (bytes / 255) and two 27-point smoothings.  colors:
+ * device uint32[n] of 0xRRGGBB for the scene's particles, NULL = white
+ * (set_object).  A box larger than the volume (the reference asserts) sets
+ * MPM_STATUS_RENDER_BOX; the particles outside are skipped. */
+int mpm_render_bake(MpmHandle* h, const void* state, int32_t scene, const uint32_t* colors,
+                    const MpmRenderVolume* vol, void* stream);
+/* render_color + next_hit (particle_sdf.py:185-217, 353-440) for one scene:
+ * per pixel the ground (view depth 0.99), the scene's tools sphere traced with
+ * their SDFs at pose (double[n_tools][8], the frame rendered), and the baked
+ * particle SDF marched with back-step refinement.  depth: float[res] view-space
+ * z of the nearest hit; normal, color: float[res][3] (colour times 3, as
+ * render_color scales it); tool_color: device float[n_tools][3]; image
+ * (nullable): float[res][3] shaded as tina's Lighting.shade_color with
+ * Diffuse (ambient 0.1 * colour + the light (1,2,3), colour 0.9, times colour / pi). */
+int mpm_render_trace(MpmHandle* h, const MpmRenderVolume* vol, const MpmRenderView* view, int32_t scene,
+                     const double* pose, const float* tool_color, float* depth, float* normal, float* color,
+                     float* image, void* stream);
 
 /* No counterpart in the reference.  One forward substep (as mpm_substep_fwd)
  * of a single scene that allocates nothing, for callers that cannot call

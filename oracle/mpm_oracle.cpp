@@ -2105,4 +2105,279 @@ double oracle_contact_min(const OracleTool* tool, const double* pose, int64_t n,
   return md;
 }
 
+// ----------------------------------------------------------------------------
+// Particle-SDF renderer (taichi_three/tina/core/particle_sdf.py), FP32 as the
+// reference's f32 fields; every operation rounded on its own.
+// ----------------------------------------------------------------------------
+}  // extern "C"
+namespace {
+struct F3 {
+  float x, y, z;
+};
+inline F3 f3(float a, float b, float c) { return F3{a, b, c}; }
+inline F3 fadd(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline F3 fsub(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline F3 fmul(F3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+inline float fdot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline float fcomp(F3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+inline F3 fnormalized(F3 a) {  // taichi: (1 / norm) * v
+  float inv = 1.0f / std::sqrt(fdot(a, a));
+  return fmul(a, inv);
+}
+// mapply_pos (tina/common.py:169-183), M row-major 4x4
+inline F3 fmapply(const float* M, F3 p) {
+  float r[3];
+  for (int i = 0; i < 3; ++i) r[i] = M[4 * i + 3] + M[4 * i] * p.x + M[4 * i + 1] * p.y + M[4 * i + 2] * p.z;
+  float w = M[15] + M[12] * p.x + M[13] * p.y + M[14] * p.z;
+  return f3(r[0] / w, r[1] / w, r[2] / w);
+}
+struct RVol {
+  const float* sdf;
+  const float* color;
+  float b0[3], b1[3];
+  int res[3];
+  float thr;
+};
+// sample_tex (particle_sdf.py:271-290)
+void rsample_tex(const float* tex, int nc, const int* res, const float* q, float* out) {
+  float pos[3], fx[3];
+  int b[3], b1[3];
+  for (int c = 0; c < 3; ++c) {
+    pos[c] = q[c] * (float)res[c];
+    int t = (int)pos[c];
+    b[c] = std::min(t, res[c] - 1);
+    fx[c] = pos[c] - (float)b[c];
+    b1[c] = std::min(b[c] + 1, res[c] - 1);
+  }
+  auto at = [&](int x, int y, int z, int ch) { return tex[(((int64_t)x * res[1] + y) * res[2] + z) * nc + ch]; };
+  for (int ch = 0; ch < nc; ++ch) {
+    float c00 = at(b[0], b[1], b[2], ch) * (1 - fx[0]) + at(b1[0], b[1], b[2], ch) * fx[0];
+    float c01 = at(b[0], b[1], b1[2], ch) * (1 - fx[0]) + at(b1[0], b[1], b1[2], ch) * fx[0];
+    float c10 = at(b[0], b1[1], b[2], ch) * (1 - fx[0]) + at(b1[0], b1[1], b[2], ch) * fx[0];
+    float c11 = at(b[0], b1[1], b1[2], ch) * (1 - fx[0]) + at(b1[0], b1[1], b1[2], ch) * fx[0];
+    float c0 = c00 * (1 - fx[1]) + c10 * fx[1];
+    float c1 = c01 * (1 - fx[1]) + c11 * fx[1];
+    out[ch] = c0 * (1 - fx[2]) + c1 * fx[2];
+  }
+}
+bool rcoord(const RVol& V, F3 p, float* q) {
+  for (int c = 0; c < 3; ++c) q[c] = (fcomp(p, c) - V.b0[c]) / (V.b1[c] - V.b0[c]);
+  return std::min(q[0], std::min(q[1], q[2])) >= 0.0f && std::max(q[0], std::max(q[1], q[2])) <= 1.0f;
+}
+float rsdf(const RVol& V, F3 p) {
+  float q[3], s = 0.0f;
+  if (rcoord(V, p, q)) {
+    rsample_tex(V.sdf, 1, V.res, q, &s);
+    s = s - V.thr;
+  }
+  return s;
+}
+F3 rcolor(const RVol& V, F3 p) {
+  float q[3], c[3] = {0, 0, 0};
+  if (rcoord(V, p, q)) rsample_tex(V.color, 3, V.res, q, c);
+  return f3(c[0], c[1], c[2]);
+}
+F3 rnormal(const RVol& V, F3 p) {
+  const float d = 1e-3f;
+  float n[3];
+  for (int i = 0; i < 3; ++i) {
+    F3 inc = p, dec = p;
+    if (i == 0) { inc.x += d; dec.x -= d; }
+    if (i == 1) { inc.y += d; dec.y -= d; }
+    if (i == 2) { inc.z += d; dec.z -= d; }
+    n[i] = (0.5f / d) * (rsdf(V, inc) - rsdf(V, dec));
+  }
+  return fnormalized(f3(n[0], n[1], n[2]));
+}
+}  // namespace
+extern "C" {
+// plb_set_particles + build_sdf_from_particles (particle_sdf.py:548-568, 237-265).
+// x: double[n][3] (cast to f32); colors: uint32[n] 0xRRGGBB or null (white).
+// sdf: float[res], color: float[res][3], bbox: float[6].  Returns 1 if the
+// particles' box exceeds the volume (the reference asserts), else 0.
+int oracle_render_bake(int64_t n, const double* x, const uint32_t* colors, const int* res, int bake_size, double dx,
+                       float* sdf, float* color, float* bbox) {
+  const float dxf = (float)dx, inv_dx = (float)(1.0 / dx);
+  float lo[3] = {1e10f, 1e10f, 1e10f}, hi[3] = {-1e10f, -1e10f, -1e10f};
+  for (int64_t i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c) {
+      float v = (std::floor((float)x[3 * i + c] * inv_dx) - 6.0f) * dxf;
+      lo[c] = std::min(lo[c], v);
+      hi[c] = std::max(hi[c], v);
+    }
+  int over = 0;
+  for (int c = 0; c < 3; ++c) {
+    if (!(((double)hi[c] - (double)lo[c]) / dx < (double)res[c])) over = 1;
+    bbox[c] = lo[c];
+    bbox[3 + c] = (float)((double)lo[c] + (double)res[c] * dx);
+  }
+  if (n == 0) over = 1;
+  const int64_t nv = (int64_t)res[0] * res[1] * res[2];
+  std::vector<int64_t> vol(nv, (int64_t)0xFFFFFFFF);  // (((1 << 31) - 1) + 1) * 2 - 1
+  for (int64_t i = 0; i < n; ++i) {
+    float p[3];
+    int coord[3];
+    for (int c = 0; c < 3; ++c) {
+      p[c] = ((float)x[3 * i + c] - bbox[c]) * inv_dx;
+      coord[c] = (int)p[c];
+    }
+    const int64_t col = colors ? (int64_t)colors[i] : 0xFFFFFF;
+    for (int a = -bake_size - 1; a < bake_size + 1; ++a)
+      for (int b = -bake_size - 1; b < bake_size + 1; ++b)
+        for (int c = -bake_size - 1; c < bake_size + 1; ++c) {
+          int ix = coord[0] + a, iy = coord[1] + b, iz = coord[2] + c;
+          if (ix < 0 || iy < 0 || iz < 0 || ix >= res[0] || iy >= res[1] || iz >= res[2]) continue;
+          float d0 = (float)ix - p[0], d1 = (float)iy - p[1], d2 = (float)iz - p[2];
+          float dist = std::sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+          float q = std::min(std::max(0.0f, 51.0f * dist), 255.0f);
+          int64_t v = ((int64_t)q << 24) + col;
+          int64_t& t = vol[((int64_t)ix * res[1] + iy) * res[2] + iz];
+          if (v < t) t = v;
+        }
+  }
+  std::vector<float> s0(nv), s1(nv);
+  for (int64_t i = 0; i < nv; ++i) {
+    int64_t c = vol[i];
+    for (int j = 2; j >= 0; --j) {
+      color[3 * i + j] = (float)(c & 255) / 255.0f;
+      c >>= 8;
+    }
+    s0[i] = (float)(c & 255) / 255.0f;
+  }
+  auto smooth = [&](const std::vector<float>& in, float* out) {
+    for (int x0 = 0; x0 < res[0]; ++x0)
+      for (int y0 = 0; y0 < res[1]; ++y0)
+        for (int z0 = 0; z0 < res[2]; ++z0) {
+          int64_t id = ((int64_t)x0 * res[1] + y0) * res[2] + z0;
+          if (x0 >= 1 && y0 >= 1 && z0 >= 1 && x0 < res[0] - 1 && y0 < res[1] - 1 && z0 < res[2] - 1) {
+            float sum = 0.0f;
+            for (int a = -1; a < 2; ++a)
+              for (int b = -1; b < 2; ++b)
+                for (int c = -1; c < 2; ++c) sum += in[((int64_t)(x0 + a) * res[1] + (y0 + b)) * res[2] + (z0 + c)];
+            out[id] = sum / 27.0f;
+          } else {
+            out[id] = 1.0f;
+          }
+        }
+  };
+  smooth(s0, s1.data());
+  smooth(s1, sdf);
+  return over;
+}
+// render_color + next_hit (particle_sdf.py:185-217, 353-440) per pixel; cam =
+// V2W[16] then W2V[16]; tools at pose; tool_color [T][3].  Outputs as
+// mpm_render_trace: depth [rx][ry], normal / color / image [rx][ry][3].
+void oracle_render_trace(const float* sdf, const float* color, const float* bbox, const int* res, float thr,
+                         const float* cam, int rx, int ry, float biasx, float biasy, const OracleTool* tools, int T,
+                         const double* pose, const float* tool_color, int show_particles, float* depth, float* normal,
+                         float* color_out, float* image) {
+  RVol V;
+  V.sdf = sdf;
+  V.color = color;
+  for (int c = 0; c < 3; ++c) {
+    V.b0[c] = bbox[c];
+    V.b1[c] = bbox[3 + c];
+    V.res[c] = res[c];
+  }
+  V.thr = thr;
+  const float* V2W = cam;
+  const float* W2V = cam + 16;
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t pix = 0; pix < (int64_t)rx * ry; ++pix) {
+    int px = (int)(pix / ry), py = (int)(pix % ry);
+    float u = ((float)px + biasx) / (float)rx * 2.0f - 1.0f;
+    float w = ((float)py + biasy) / (float)ry * 2.0f - 1.0f;
+    F3 Pl = fmapply(V2W, f3(u, w, 1.0f)), o = fmapply(V2W, f3(u, w, 0.0f));
+    F3 d = fnormalized(fsub(Pl, o));
+    float closest = 0.99f;
+    F3 nrm = f3(0, 1, 0), col = f3(0.3f * 0.3f, 0.5f * 0.3f, 0.7f * 0.3f);
+    if (T > 0) {
+      int j = 0, sid = 0;
+      float dist = 0.0f, sval = 1e10f;
+      F3 pp = o;
+      while (j < 200 && dist < 100.0f && sval > 1e-8f) {
+        pp = fadd(o, fmul(d, dist));
+        sval = 1e10f;
+        for (int i = 0; i < T; ++i) {
+          const double q[3] = {pp.x, pp.y, pp.z};
+          float dd = (float)tool_sdf(tools[i], pose + 8 * i, q);
+          if (dd < sval) {
+            sval = dd;
+            sid = i;
+          }
+        }
+        dist += sval;
+        ++j;
+      }
+      float dz = fmapply(W2V, pp).z;
+      if (dz < closest && dz < 100.0f) {
+        closest = dz;
+        F3 h = fadd(o, fmul(d, dist));
+        const double q[3] = {h.x, h.y, h.z};
+        double n[3];
+        tool_normal(tools[sid], pose + 8 * sid, q, n);
+        nrm = f3((float)n[0], (float)n[1], (float)n[2]);
+        col = f3(tool_color[3 * sid], tool_color[3 * sid + 1], tool_color[3 * sid + 2]);
+      }
+    }
+    if (show_particles) {
+      // ray_aabb_intersection (renderer_utils.py:53-73)
+      bool hit = true;
+      float tn = -1e10f, tf = 1e10f;
+      for (int i = 0; i < 3; ++i) {
+        float oi = fcomp(o, i), di = fcomp(d, i);
+        if (di == 0.0f) {
+          if (oi < V.b0[i] || oi > V.b1[i]) hit = false;
+        } else {
+          float i1 = (V.b0[i] - oi) / di, i2 = (V.b1[i] - oi) / di;
+          float nf = (i2 < i1) ? i1 : i2, nn = (i1 < i2) ? i1 : i2;
+          tf = (nf < tf) ? nf : tf;
+          tn = (tn < nn) ? nn : tn;
+        }
+      }
+      if (tn > tf) hit = false;
+      if (hit) {
+        tn = (0.0f < tn) ? tn : 0.0f;
+        F3 pos = fadd(o, fmul(d, tn + 1e-4f)), step = f3(0, 0, 0);
+        for (int j = 0; j < 500; ++j) {
+          float s = rsdf(V, pos);
+          if (s < 0.0f) {
+            F3 back = step;
+            for (int k = 0; k < 20; ++k) {
+              back = fmul(back, 0.5f);
+              if (rsdf(V, fsub(pos, back)) < 0.0f) pos = fsub(pos, back);
+            }
+            float dz = fmapply(W2V, pos).z;
+            if (dz < closest) {
+              closest = dz;
+              nrm = rnormal(V, pos);
+              col = rcolor(V, pos);
+            }
+            break;
+          }
+          float a = s * 0.005f;
+          step = fmul(d, (a < 0.002f) ? 0.002f : a);
+          pos = fadd(pos, step);
+        }
+      }
+    }
+    col = fmul(col, 3.0f);
+    depth[pix] = closest;
+    normal[3 * pix] = nrm.x;
+    normal[3 * pix + 1] = nrm.y;
+    normal[3 * pix + 2] = nrm.z;
+    color_out[3 * pix] = col.x;
+    color_out[3 * pix + 1] = col.y;
+    color_out[3 * pix + 2] = col.z;
+    if (image) {
+      float il = 1.0f / std::sqrt(14.0f);
+      float cos_i = nrm.x * il + nrm.y * (2.0f * il) + nrm.z * (3.0f * il);
+      float lam = cos_i > 0.0f ? cos_i * 0.9f * (1.0f / 3.14159265358979f) : 0.0f;
+      image[3 * pix] = 0.1f * col.x + lam * col.x;
+      image[3 * pix + 1] = 0.1f * col.y + lam * col.y;
+      image[3 * pix + 2] = 0.1f * col.z + lam * col.z;
+    }
+  }
+}
+
 }  // extern "C"

@@ -84,6 +84,9 @@ def lib():
         L.oracle_contact_min.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int64, _dp, ctypes.c_double, _dp, _dp,
                                          ctypes.POINTER(ctypes.c_int64)]
         L.oracle_collision_pairs.restype = ctypes.c_int
+        L.oracle_render_bake.restype = ctypes.c_int
+        L.oracle_render_bake.argtypes = [ctypes.c_int64, _dp, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                         ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.oracle_target_sdf_f64.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp, _dp, _dp]
         _fp = ctypes.POINTER(ctypes.c_float)
         L.oracle_target_sdf_f32.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, _fp, _fp, _fp]
@@ -183,6 +186,45 @@ def iou(grid_m: np.ndarray, target: np.ndarray) -> float:
     inter = float(np.sum(a * b)) / ma / mb
     union = float(a.sum()) / ma + float(b.sum()) / mb
     return inter / (union - inter)
+
+
+def render_bake(x: np.ndarray, res=(168, 168, 168), bake_size: int = 6, dx: float = 1 / 150, colors=None):
+    """``plb_set_particles`` + ``build_sdf_from_particles`` (particle_sdf.py:548-568,
+    237-265) in FP32: returns (sdf (res), color (res + (3,)), bbox (2, 3), over)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    r = np.asarray(res, dtype=np.int32)
+    sdf = np.empty(tuple(res), dtype=np.float32)
+    color = np.empty(tuple(res) + (3,), dtype=np.float32)
+    bbox = np.empty(6, dtype=np.float32)
+    cols = None if colors is None else np.ascontiguousarray(colors, dtype=np.uint32)
+    over = lib().oracle_render_bake(x.shape[0], ptr(x), None if cols is None else cols.ctypes.data_as(ctypes.c_void_p),
+                                    r.ctypes.data_as(ctypes.c_void_p), int(bake_size), float(dx),
+                                    sdf.ctypes.data_as(ctypes.c_void_p), color.ctypes.data_as(ctypes.c_void_p),
+                                    bbox.ctypes.data_as(ctypes.c_void_p))
+    return sdf, color, bbox.reshape(2, 3), int(over)
+
+
+def render_trace(sdf, color, bbox, v2w, w2v, img_res, sdf_threshold=0.37 * 0.56, tools=(), pose=None,
+                 tool_color=None, show_particles=True, bias=(0.5, 0.5), softness=666.0):
+    """``render_color`` + ``next_hit`` (particle_sdf.py:185-217, 353-440) per pixel, FP32:
+    returns depth (rx, ry), normal, color, image (rx, ry, 3)."""
+    rx, ry = img_res
+    res = np.asarray(sdf.shape, dtype=np.int32)
+    cam = np.concatenate([np.asarray(v2w, np.float32).ravel(), np.asarray(w2v, np.float32).ravel()])
+    T = len(tools)
+    arr = (OracleToolStruct * max(T, 1))()
+    for i, t in enumerate(tools):
+        arr[i] = tool_struct(t, softness)
+    pose = np.zeros((max(T, 1), 8)) if pose is None else np.ascontiguousarray(pose, dtype=np.float64)
+    tc = np.zeros((max(T, 1), 3), np.float32) if tool_color is None else np.ascontiguousarray(tool_color, np.float32)
+    depth = np.empty((rx, ry), np.float32)
+    nrm, col, img = (np.empty((rx, ry, 3), np.float32) for _ in range(3))
+    vp = lambda a: np.ascontiguousarray(a).ctypes.data_as(ctypes.c_void_p)
+    lib().oracle_render_trace(vp(np.ascontiguousarray(sdf, np.float32)), vp(np.ascontiguousarray(color, np.float32)),
+                              vp(np.asarray(bbox, np.float32).ravel()), vp(res), ctypes.c_float(sdf_threshold),
+                              vp(cam), int(rx), int(ry), ctypes.c_float(bias[0]), ctypes.c_float(bias[1]), arr, T,
+                              ptr(pose), vp(tc), int(bool(show_particles)), vp(depth), vp(nrm), vp(col), vp(img))
+    return depth, nrm, col, img
 
 
 class Oracle:

@@ -564,3 +564,35 @@ def test_collision_projection_adjoint_matches_finite_differences():
         fds = _fd_best(f, a, k, (1e-6, 1e-7))
         best = min(abs(v - flat[k]) / max(abs(v), 1e-6) for v in fds)
         assert best < 1e-5, (k, flat[k], fds)
+
+
+# --------------------------------------------------------------------------
+# particle-SDF renderer (tina/core/particle_sdf.py)
+# --------------------------------------------------------------------------
+def test_tina_camera_looks_at_its_center():
+    from diffskill_gb300.render import tina_camera
+    w2v, v2w = tina_camera((0.5, 0.0, 0.5), 0.0, -0.8, 0.88)
+    c = w2v.astype(np.float64) @ np.array([0.5, 0.0, 0.5, 1.0])
+    assert abs(c[0] / c[3]) < 1e-6 and abs(c[1] / c[3]) < 1e-6  # the center projects to the image center
+    eye = v2w.astype(np.float64) @ np.array([0.0, 0.0, -1.0, 1.0])  # a point on the near plane
+    eye = eye[:3] / eye[3]
+    assert abs(np.linalg.norm(eye - np.array([0.5, 0.0, 0.5])) - (0.88 - 0.05)) < 1e-3
+    assert np.allclose(np.linalg.inv(w2v.astype(np.float64)), v2w, atol=1e-4)
+
+
+def test_render_bake_volume():
+    """The baked SDF is the smoothed, quantised distance to the nearest particle:
+    low around particles, 1 far away; the box starts 6 voxels below the particles."""
+    rng = np.random.default_rng(1)
+    x = np.array([0.5, 0.3, 0.5]) + rng.uniform(-0.05, 0.05, size=(400, 3))
+    dx = 1 / 150
+    sdf, color, bbox, over = O.render_bake(x, (48, 48, 48), 6, dx)
+    assert over == 0
+    assert np.allclose(bbox[0], (np.floor((x.astype(np.float32) * np.float32(150)).min(0)) - 6) * np.float32(dx))
+    assert np.allclose(bbox[1], bbox[0] + 48 * dx, atol=1e-6)
+    idx = ((x.astype(np.float32) - bbox[0]) * np.float32(150)).astype(int)
+    v = sdf[tuple(idx.T)]  # 0.2 per voxel of distance (51 / 255), smoothed; particles ~2 voxels apart
+    assert v.max() < 0.45 and np.median(v) < 0.3 and sdf[0, 0, 0] == 1.0 and sdf[47, 47, 47] == 1.0
+    assert (color == 1.0).all()  # white particles, white empty voxels
+    # an undersized volume is reported
+    assert O.render_bake(x, (12, 12, 12), 6, dx)[3] == 1
