@@ -428,3 +428,21 @@ def test_collision_trajectory_loss_and_grad(gpu_lib):
     torch.cuda.synchronize()
     assert abs(loss - loss_ref) < 1e-12 * abs(loss_ref)
     assert rel_err(g, grad_ref) < 1e-8
+
+
+@pytest.mark.parametrize("prec,loss_tol,grad_tol", [("fp64", 1e-9, 1e-6), ("fp32_svd64", 1e-3, 5e-2)])
+def test_config4_grid128_knife_gripper_trajectory(gpu_lib, prec, loss_tol, grad_tol):
+    """Config-4 shape on the 128^3 grid: knife (box ∩ prism) and gripper, density
+    L1 to the two half piles plus the soft contact term, against the oracle."""
+    from diffskill_gb300 import scenes
+    sc = scenes.config4(n_actions=2, n_particles=12000, substeps=10, precision=prec)
+    assert sc.sim.grid == 128
+    o = Oracle(sc.sim, sc.tools)
+    ref_loss, ref_grad = o.loss_and_grad(sc.x0, sc.actions, sc.target, density_weight=sc.density_weight,
+                                         contact_weight=sc.contact_weight)
+    eng = make_engine(sc)
+    loss, grad, _ = _traj(eng, sc, k=5)
+    assert eng.status() == 0
+    assert abs(loss - ref_loss) / abs(ref_loss) < loss_tol, (loss, ref_loss)
+    assert np.abs(ref_grad).max() > 0
+    assert rel_err(grad, ref_grad) < grad_tol, (grad, ref_grad)
