@@ -449,6 +449,9 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 6 : 
   zero_stencil(s);
   bool ok = false;
   int scene = 0;
+  // node value of stencil offset o: wgt(o) * (pm + affine o), where
+  // affine = dx A and pm = m v - affine fx (= m v + A dp at o = 0, dp = (o - fx) dx);
+  // stepped across the stencil by additions of affine's columns
   T affine[9], pm[3] = {T(0), T(0), T(0)};
 #pragma unroll
   for (int k = 0; k < 9; ++k) affine[k] = T(0);
@@ -476,9 +479,10 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 6 : 
     if (ok) {
       scene = pscene[p];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) affine[k] = T(aff[k]);
+      for (int k = 0; k < 9; ++k) affine[k] = T(aff[k]) * c.dx;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) pm[k] = c.p_mass * v[k];
+      for (int k = 0; k < 3; ++k)
+        pm[k] = c.p_mass * v[k] - (affine[3 * k] * s.fx[0] + affine[3 * k + 1] * s.fx[1] + affine[3 * k + 2] * s.fx[2]);
     } else {
       zero_stencil(s);
     }
@@ -503,21 +507,21 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 6 : 
   } else {
     seg = warp_segments(key);
   }
+  T cx[3] = {pm[0], pm[1], pm[2]};
 #pragma unroll 1
   for (int ox = 0; ox < 3; ++ox) {
     const T wx = sel3(s.w[0][0], s.w[1][0], s.w[2][0], ox);
     const int ax = sel3(A.ax[0], A.ax[1], A.ax[2], ox);
-    const T dpx = (T(ox) - s.fx[0]) * c.dx;
+    T cy[3] = {cx[0], cx[1], cx[2]};
 #pragma unroll
-    for (int oy = 0; oy < 3; ++oy)
+    for (int oy = 0; oy < 3; ++oy) {
+      T cz[3] = {cy[0], cy[1], cy[2]};
 #pragma unroll
       for (int oz = 0; oz < 3; ++oz) {
         const T wgt = wx * s.w[oy][1] * s.w[oz][2];
-        const T dp[3] = {dpx, (T(oy) - s.fx[1]) * c.dx, (T(oz) - s.fx[2]) * c.dx};
         T mv[4];
 #pragma unroll
-        for (int k = 0; k < 3; ++k)
-          mv[k] = wgt * (pm[k] + affine[3 * k] * dp[0] + affine[3 * k + 1] * dp[1] + affine[3 * k + 2] * dp[2]);
+        for (int k = 0; k < 3; ++k) mv[k] = wgt * cz[k];
         mv[3] = wgt * c.p_mass;
         if constexpr (slab) {
           sb->v[lane][oy * 3 + oz] = make_float4(mv[0], mv[1], mv[2], mv[3]);
@@ -528,7 +532,14 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 6 : 
           }
           if (ok && seg.tail) atomic_add_node(g + ax + A.ay[oy] + A.az[oz], mv[0], mv[1], mv[2], mv[3]);
         }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) cz[k] += affine[3 * k + 2];
       }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) cy[k] += affine[3 * k + 1];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) cx[k] += affine[3 * k];
     if constexpr (slab) {
       sb->base[lane] = g + ax;
       __syncwarp();
@@ -823,23 +834,33 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 2) k_g2p_adj(Consts<
   for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int b = 0; b < 3; ++b) gw[a][b] = T(0);
-  T gfx[3] = {T(0), T(0), T(0)};
+  // the x-derivative through dp = o - fx of sum_o wgt gv(o) . (k4 gC dp) is
+  // -k4 gC^T sum_o wgt gv(o) = -k4 gC^T new_v
+  T gfx[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) gfx[j] = -k4 * (gC[j] * nv[0] + gC[3 + j] * nv[1] + gC[6 + j] * nv[2]);
+  // u(o) = gnv + k4 gC (o - fx): the node value is wgt(o) u(o) and the weight
+  // adjoint gv(o) . u(o); u is stepped across the stencil by the columns of k4 gC
+  T ux[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) gC[3 * i + j] *= k4;
+    ux[i] = gnv[i] - (gC[3 * i] * s.fx[0] + gC[3 * i + 1] * s.fx[1] + gC[3 * i + 2] * s.fx[2]);
+  }
 #pragma unroll 1
   for (int ox = 0; ox < 3; ++ox) {
     const T wx = sel3(s.w[0][0], s.w[1][0], s.w[2][0], ox);
     const int ax = sel3(A.ax[0], A.ax[1], A.ax[2], ox);
-    const T dpx = T(ox) - s.fx[0];
     T gwx = T(0);
+    T uy[3] = {ux[0], ux[1], ux[2]};
 #pragma unroll
-    for (int oy = 0; oy < 3; ++oy)
+    for (int oy = 0; oy < 3; ++oy) {
+      T uz[3] = {uy[0], uy[1], uy[2]};
 #pragma unroll
       for (int oz = 0; oz < 3; ++oz) {
         const T wgt = wx * s.w[oy][1] * s.w[oz][2];
-        const T dp[3] = {dpx, T(oy) - s.fx[1], T(oz) - s.fx[2]};
-        T gCd[3];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) gCd[i] = gC[3 * i] * dp[0] + gC[3 * i + 1] * dp[1] + gC[3 * i + 2] * dp[2];
-        T sc3[3] = {wgt * (gnv[0] + k4 * gCd[0]), wgt * (gnv[1] + k4 * gCd[1]), wgt * (gnv[2] + k4 * gCd[2])};
+        T sc3[3] = {wgt * uz[0], wgt * uz[1], wgt * uz[2]};
         if constexpr (slab) {
           sb->v[lane][oy * 3 + oz] = make_float4(sc3[0], sc3[1], sc3[2], 0.f);
         } else if (seg.steps) {
@@ -853,15 +874,19 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 2) k_g2p_adj(Consts<
           }
           Node<T> n = g[a];
           const T gv[3] = {n.x, n.y, n.z};
-          T g_wgt = dot3(gv, gnv) + k4 * dot3(gv, gCd);
-#pragma unroll
-          for (int j = 0; j < 3; ++j)
-            gfx[j] -= k4 * wgt * (gC[j] * gv[0] + gC[3 + j] * gv[1] + gC[6 + j] * gv[2]);
+          T g_wgt = dot3(gv, uz);
           gwx += g_wgt * s.w[oy][1] * s.w[oz][2];
           gw[oy][1] += g_wgt * wx * s.w[oz][2];
           gw[oz][2] += g_wgt * wx * s.w[oy][1];
         }
+#pragma unroll
+        for (int i = 0; i < 3; ++i) uz[i] += gC[3 * i + 2];
       }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) uy[i] += gC[3 * i + 1];
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) ux[i] += gC[3 * i];
     add3(gw[0][0], gw[1][0], gw[2][0], ox, gwx);
     if constexpr (slab) {
       sb->base[lane] = gg + ax;
@@ -1027,35 +1052,52 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 4 : 
     for (int a = 0; a < 3; ++a)
 #pragma unroll
       for (int b = 0; b < 3; ++b) gw[a][b] = T(0);
-    T gfx[3] = {T(0), T(0), T(0)};
+    // q(o) = wgt(o) gn(o) and sq = sum_o q(o): the adjoints of m v (gv = m sq) and of
+    // dp = (o - fx) dx through A dp (gfx = -dx A^T sq) need only the sum; the node
+    // value m v + A dp is stepped across the stencil by the columns of dx A
+    T sq[3] = {T(0), T(0), T(0)};
+    T ad[9], cx[3];
 #pragma unroll
-    for (int ox = 0; ox < 3; ++ox)
+    for (int k = 0; k < 9; ++k) ad[k] = affine[k] * c.dx;
 #pragma unroll
-      for (int oy = 0; oy < 3; ++oy)
+    for (int k = 0; k < 3; ++k) cx[k] = c.p_mass * v[k] - (ad[3 * k] * s.fx[0] + ad[3 * k + 1] * s.fx[1] + ad[3 * k + 2] * s.fx[2]);
+#pragma unroll
+    for (int ox = 0; ox < 3; ++ox) {
+      T cy[3] = {cx[0], cx[1], cx[2]};
+#pragma unroll
+      for (int oy = 0; oy < 3; ++oy) {
+        T cz[3] = {cy[0], cy[1], cy[2]};
 #pragma unroll
         for (int oz = 0; oz < 3; ++oz) {
           T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
           const T dp[3] = {(T(ox) - s.fx[0]) * c.dx, (T(oy) - s.fx[1]) * c.dx, (T(oz) - s.fx[2]) * c.dx};
           Node<T> n = gg[A.at(ox, oy, oz)];
           const T gn[3] = {n.x, n.y, n.z};
-          T contrib[3];
-#pragma unroll
-          for (int k = 0; k < 3; ++k)
-            contrib[k] = c.p_mass * v[k] + affine[3 * k] * dp[0] + affine[3 * k + 1] * dp[1] + affine[3 * k + 2] * dp[2];
-          T g_wgt = dot3(gn, contrib) + n.w * c.p_mass;
+          T g_wgt = dot3(gn, cz) + n.w * c.p_mass;
 #pragma unroll
           for (int k = 0; k < 3; ++k) {
-            gv[k] += wgt * c.p_mass * gn[k];
+            const T q = wgt * gn[k];
+            sq[k] += q;
 #pragma unroll
-            for (int j = 0; j < 3; ++j) ga[3 * k + j] += wgt * gn[k] * dp[j];
+            for (int j = 0; j < 3; ++j) ga[3 * k + j] += q * dp[j];
           }
-#pragma unroll
-          for (int j = 0; j < 3; ++j)
-            gfx[j] -= c.dx * wgt * (affine[j] * gn[0] + affine[3 + j] * gn[1] + affine[6 + j] * gn[2]);
           gw[ox][0] += g_wgt * s.w[oy][1] * s.w[oz][2];
           gw[oy][1] += g_wgt * s.w[ox][0] * s.w[oz][2];
           gw[oz][2] += g_wgt * s.w[ox][0] * s.w[oy][1];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) cz[k] += ad[3 * k + 2];
         }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) cy[k] += ad[3 * k + 1];
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) cx[k] += ad[3 * k];
+    }
+    T gfx[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) gfx[j] = -(ad[j] * sq[0] + ad[3 + j] * sq[1] + ad[6 + j] * sq[2]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) gv[k] = c.p_mass * sq[k];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
 #pragma unroll
