@@ -9,7 +9,8 @@ template <typename T>
 Consts<T> make_consts(const LaunchCtx& L);  // mpm_fwd.cu
 template <typename T>
 cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* b,
-                           const MpmGridStore* store, int slot);
+                           const MpmGridStore* restore, int restore_slot, const MpmGridStore* reserve,
+                           int reserve_slot);
 unsigned grid_blocks_launch(const LaunchCtx& L, int64_t total_blocks);
 
 static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
@@ -27,11 +28,15 @@ cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* st1, c
   const unsigned pb = blocks_for(c.n_particles, 128);
   const unsigned gb = grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3);
   // recompute the grid of this substep (substep_grad, mpm_simulator.py:327-333)
-  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, g_gout, store, slot);
+  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, g_gout, store, slot, nullptr, -1);
   if (e != cudaSuccess) return e;
-  if (c.n_particles > 0)
-    MPM_LAUNCH(L, MPM_K_P2G_RECOMP, (k_p2g<T, S>), pb, 128, c, st0, (T*)nullptr, L.pscene, gin,
-               store ? store->slot_start + slot : (const int64_t*)nullptr);
+  if (c.n_particles > 0) {
+    // with a grid store the recompute usually exits at once: a grid of one
+    // wave of CTAs that stride over the particles
+    const unsigned cap = (unsigned)(L.sm_count * 6);
+    MPM_LAUNCH(L, MPM_K_P2G_RECOMP, (k_p2g<T, S, true>), store && pb > cap ? cap : pb, 128, c, st0, (T*)nullptr,
+               L.pscene, gin, store ? store->slot_start + slot : (const int64_t*)nullptr);
+  }
   MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, gb, 64, c, L.active, counter, gin, gout, L.tools, L.tool_off, pose_f,
              pose_f1);
   if (c.n_particles > 0)

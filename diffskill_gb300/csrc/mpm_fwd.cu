@@ -37,31 +37,40 @@ template Consts<double> make_consts<double>(const LaunchCtx&);
 
 static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
-// Active blocks of frame st: clear flags, mark, compact, then zero the listed
-// blocks of grid a (and b if given).  Leaves the list in L.active and its
-// length at L.blockbuf[0..3].
-// ``saved`` (device, may be null): when it points at a slot start >= 0 the
-// list and grid a were restored from the grid store and are kept.
+// Active blocks of frame st: clear flags, mark, then compact the list and
+// zero the listed blocks of grid a (and b if given).  Leaves the list in
+// L.active and its length at L.blockbuf[0..3] (a ticket counter at [4..7]).
+// ``restore`` (may be null): the adjoint's grid store; when its slot holds
+// this substep the list and grid a are restored from it and b is zeroed.
+// ``reserve`` (may be null): the forward's grid store; room for the list is
+// reserved in slot ``reserve_slot`` by the compaction's last CTA.
 template <typename T>
 cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* b,
-                           const MpmGridStore* store, int slot) {
+                           const MpmGridStore* restore, int restore_slot, const MpmGridStore* reserve,
+                           int reserve_slot) {
   const int64_t total = (int64_t)c.n_scenes * c.NB3;
   int* counter = reinterpret_cast<int*>(L.blockbuf);
+  unsigned* ticket = reinterpret_cast<unsigned*>(L.blockbuf + 4);
   unsigned char* flags = L.blockbuf + 16;
-  const int64_t* saved = store ? store->slot_start + slot : nullptr;
+  const int64_t* saved = restore ? restore->slot_start + restore_slot : nullptr;
   MPM_MEMSET(L, L.blockbuf, blockbuf_bytes(c.n_scenes, c.n_grid));
-  if (store)
-    MPM_LAUNCH(L, MPM_K_CLEAR, k_store_restore<T>, (unsigned)(L.sm_count * 8), 256, *store, slot, L.active, counter, a);
-  if (c.n_particles > 0)
-    MPM_LAUNCH(L, MPM_K_CLEAR, k_mark_blocks<T>, blocks_for(c.n_particles, 256), 256, c, st, L.pscene, flags, saved);
-  MPM_LAUNCH(L, MPM_K_CLEAR, k_compact_blocks, blocks_for(total, 256), 256, flags, total, L.active, counter, saved);
-  MPM_LAUNCH(L, MPM_K_CLEAR, k_clear_blocks<T>, (unsigned)(L.sm_count * 8), 256, L.active, counter, a, b, saved);
+  if (restore)
+    MPM_LAUNCH(L, MPM_K_CLEAR, k_store_restore<T>, (unsigned)(L.sm_count * 8), 256, *restore, restore_slot,
+               L.active, counter, a, b);
+  if (c.n_particles > 0) {
+    const unsigned mb = blocks_for(c.n_particles, 256), cap = (unsigned)(L.sm_count * 16);
+    MPM_LAUNCH(L, MPM_K_CLEAR, k_mark_blocks<T>, mb < cap ? mb : cap, 256, c, st, L.pscene, flags, saved);
+  }
+  MpmGridStore rs{};
+  if (reserve) rs = *reserve;
+  MPM_LAUNCH(L, MPM_K_CLEAR, k_compact_clear<T>, blocks_for(total, 256), 256, flags, total, L.active, counter, ticket,
+             a, b, saved, rs, reserve ? reserve_slot : -1);
   return cudaGetLastError();
 }
 template cudaError_t prepare_blocks<float>(const LaunchCtx&, const Consts<float>&, const float*, Node<float>*,
-                                           Node<float>*, const MpmGridStore*, int);
+                                           Node<float>*, const MpmGridStore*, int, const MpmGridStore*, int);
 template cudaError_t prepare_blocks<double>(const LaunchCtx&, const Consts<double>&, const double*, Node<double>*,
-                                            Node<double>*, const MpmGridStore*, int);
+                                            Node<double>*, const MpmGridStore*, int, const MpmGridStore*, int);
 
 unsigned grid_blocks_launch(const LaunchCtx& L, int64_t total_blocks) {
   int64_t g = (int64_t)L.sm_count * 16;
@@ -75,15 +84,13 @@ cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const d
   Node<T>* gin = (Node<T>*)L.grid_a;
   Node<T>* gout = (Node<T>*)L.grid_b;
   const int* counter = reinterpret_cast<const int*>(L.blockbuf);
-  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, (Node<T>*)nullptr, nullptr, -1);
+  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, (Node<T>*)nullptr, nullptr, -1, store, slot);
   if (e != cudaSuccess) return e;
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S>), blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gin,
                (const int64_t*)nullptr);
-  if (store) {
-    MPM_LAUNCH(L, MPM_K_CLEAR, k_store_reserve, 1, 1, *store, slot, counter);
+  if (store)
     MPM_LAUNCH(L, MPM_K_CLEAR, k_store_copy<T>, (unsigned)(L.sm_count * 8), 256, *store, slot, L.active, gin);
-  }
   MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3), 64, c, L.active,
              counter, gin, gout, L.tools, L.tool_off, pose_f, pose_f1);
   if (c.n_particles > 0)

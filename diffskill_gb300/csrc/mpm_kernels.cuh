@@ -17,8 +17,8 @@
 // Sparse grid: the scratch grids of a substep are stored block-contiguous
 // (blocks of 4x4x4 nodes, 64 nodes = 1 KiB in FP32 per block).  Each substep
 // marks the blocks that particle stencils touch (k_mark_blocks), compacts them
-// into a device-side list (k_compact_blocks), clears only those
-// (k_clear_blocks), and runs grid_op / grid_op.grad over that list with
+// into a device-side list and clears only those (k_compact_clear), and runs
+// grid_op / grid_op.grad over that list with
 // grid-stride loops (no host round trip; capturable in a CUDA graph).  Nodes
 // outside the list hold no mass, so grid_op leaves them at zero exactly as the
 // dense reference does; g2p and p2g.grad only read nodes inside the list.
@@ -183,16 +183,18 @@ MPM_DI void warp_tails(long long key, bool ok, unsigned& tails, unsigned& emit) 
 
 // FP32 slab scatter.  The 27-node stencil is scattered one ox slab (9 nodes)
 // at a time: every lane writes its 9 node values into row `lane` of v, then
-// lanes 0..26 read the table by columns, lane = 9 g + j summing column j over
+// lanes 0..26 read the table by columns, lane = g + 3 j summing column j over
 // rows [11 g, 11 g + 11).  Each run of equal keys closed inside a row group
 // issues one red.global.add.v4.f32 per node; the run still open at the end of
 // a group is carried into the next group by two shuffles.  This replaces a
 // shuffle scan of 4 values x 27 nodes x up to 5 steps per lane with 27
 // shared-memory stores, 11 loads per slab and 8 shuffles per slab, and keeps
-// one atomic per (run, node).  Row stride 9 x 16 B: stores and loads are
-// bank-conflict-free within each quarter warp.
+// one atomic per (run, node).  Row stride 9 x 16 B: the stores (lane l, slot
+// 9 l + n) and the loads (slot 99 g + 9 i + j, i.e. 3 g + i + j mod 8 with
+// lane = g + 3 j) fall in distinct 16-byte bank groups within each quarter
+// warp.
 struct SlabStage {
-  float4 v[32][9];
+  float4 v[33][9];  // row 32: read, never used (the open run of group 2 after row 31)
   Node<float>* base[32];  // grid of the row's scene + ax[ox] of the row's base cell
   int ay[32][3], az[32][3];
 };
@@ -212,33 +214,32 @@ MPM_DI void slab_emit(const SlabStage& sb, int r, int oy, int oz, const float4& 
 // call between two __syncwarp()s, after all lanes wrote their row of sb.v
 MPM_DI void slab_reduce(const SlabStage& sb, unsigned tails, unsigned emit) {
   const int lane = threadIdx.x & 31;
-  const int g = lane / 9;  // 3 for lanes 27..31: no rows
-  const int j = lane - 9 * g;
+  // lanes 27..31 (g = 3) read lane 24's cells (a broadcast) and emit nothing
+  const int g = lane < 27 ? lane % 3 : 3;
+  const int j = lane < 27 ? lane / 3 : 8;
   const int oy = j / 3, oz = j - 3 * (j / 3);
   const int r0 = 11 * (g < 3 ? g : 0);
-  const unsigned mine = g < 3 ? tails >> r0 : 0u;
+  const unsigned mine = g < 3 ? tails >> r0 : 0u;  // group 2: bit 10 (row 32) is 0
   float4 acc = make_float4(0.f, 0.f, 0.f, 0.f), head = acc;
   int head_row = -1;
 #pragma unroll
   for (int i = 0; i < 11; ++i) {
-    if (g < 3 && r0 + i < 32) {
-      f4_add(acc, sb.v[r0 + i][j]);
-      if ((mine >> i) & 1u) {
-        if (g > 0 && head_row < 0) {
-          head = acc;  // closes a run that may have started in the group before
-          head_row = r0 + i;
-        } else if ((emit >> (r0 + i)) & 1u) {
-          slab_emit(sb, r0 + i, oy, oz, acc);
-        }
-        acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    f4_add(acc, sb.v[r0 + i][j]);
+    if ((mine >> i) & 1u) {
+      if (g > 0 && head_row < 0) {
+        head = acc;  // closes a run that may have started in the group before
+        head_row = r0 + i;
+      } else if ((emit >> (r0 + i)) & 1u) {
+        slab_emit(sb, r0 + i, oy, oz, acc);
       }
+      acc = make_float4(0.f, 0.f, 0.f, 0.f);
     }
   }
   // acc = the open run at the group's end; group 2 always closes (row 31)
-  const float4 c1 = f4_shfl_up(acc, 9);  // group 1: open run of group 0
+  const float4 c1 = f4_shfl_up(acc, 1);  // group 1: open run of group 0
   float4 fwd = acc;
   if (g == 1 && head_row < 0) f4_add(fwd, c1);  // group 1 without a tail passes the run on
-  const float4 c2 = f4_shfl_up(fwd, 9);          // group 2: open run of groups 0..1
+  const float4 c2 = f4_shfl_up(fwd, 1);          // group 2: open run of groups 0..1
   if (g >= 1 && g < 3 && head_row >= 0) {
     f4_add(head, g == 1 ? c1 : c2);
     if ((emit >> head_row) & 1u) slab_emit(sb, head_row, oy, oz, head);
@@ -436,14 +437,10 @@ MPM_DI MatConsts<S> mat_consts(const Consts<T>& c) {
 // ---------------------------------------------------------------------------
 // forward kernels
 // ---------------------------------------------------------------------------
-// FP32: 6 CTAs of 128 threads per SM (at most 85 registers, no spill);
-// measured 8 % faster than the unconstrained 93 registers
+// one 128-particle chunk of p2g (all 128 threads of the block take part)
 template <typename T, typename S>
-__global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 6 : 4) k_p2g(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
-                                             const int* __restrict__ pscene, Node<T>* __restrict__ grid,
-                                             const int64_t* __restrict__ saved) {
-  if (saved && *saved >= 0) return;  // the grid of this substep was restored from the grid store
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+MPM_DI void p2g_chunk(const Consts<T>& c, const T* __restrict__ st, T* __restrict__ st_out,
+                      const int* __restrict__ pscene, Node<T>* __restrict__ grid, int64_t p) {
   const bool valid = p < c.n_particles;  // every lane stays for the warp scan
   Stencil<T> s;
   zero_stencil(s);
@@ -546,6 +543,22 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 6 : 
       slab_reduce(*sb, tails, emit);
       __syncwarp();
     }
+  }
+}
+// FP32: 6 CTAs of 128 threads per SM (at most 85 registers, no spill);
+// measured 8 % faster than the unconstrained 93 registers
+// Strided: the CTAs stride over the particle chunks (the adjoint's recompute,
+// which exits at once when the grid store holds the substep)
+template <typename T, typename S, bool Strided = false>
+__global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 6 : 4) k_p2g(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
+                                             const int* __restrict__ pscene, Node<T>* __restrict__ grid,
+                                             const int64_t* __restrict__ saved) {
+  if (saved && *saved >= 0) return;  // the grid of this substep was restored from the grid store
+  if constexpr (Strided) {
+    for (int64_t p0 = (int64_t)blockIdx.x * blockDim.x; p0 < c.n_particles; p0 += (int64_t)gridDim.x * blockDim.x)
+      p2g_chunk<T, S>(c, st, st_out, pscene, grid, p0 + threadIdx.x);
+  } else {
+    p2g_chunk<T, S>(c, st, st_out, pscene, grid, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
   }
 }
 
@@ -1123,60 +1136,109 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 4 : 
 // ---------------------------------------------------------------------------
 // active-block bookkeeping
 // ---------------------------------------------------------------------------
-// flags[scene*NB3 + block] = 1 for every block a particle stencil touches
+// flags[scene*NB3 + block] = 1 for every block a particle stencil touches.
+// In cell order neighbouring particles touch the same blocks, so the lanes of
+// a warp with equal (scene, block range) elect one writer (__match_any_sync):
+// about one flag store per block per warp instead of one per particle.
+// Grid-stride over warp-aligned ranges (the early exit of a restored substep
+// then costs a small grid).
 template <typename T>
 __global__ void __launch_bounds__(256) k_mark_blocks(Consts<T> c, const T* __restrict__ st,
                                                      const int* __restrict__ pscene,
                                                      unsigned char* __restrict__ flags,
                                                      const int64_t* __restrict__ saved) {
   if (saved && *saved >= 0) return;
-  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= c.n_particles) return;
-  T x[3];
-  load_row(st, c.ld, p, 0, 3, x);
-  Stencil<T> s;
-  if (!make_stencil(c, x, s)) return;  // skipped (and flagged) by the scatter
-  int lo[3], hi[3];
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p - lane < c.n_particles; p += stride) {
+    bool ok = false;
+    int scene = 0, lo[3] = {0, 0, 0}, ext[3] = {0, 0, 0};
+    unsigned long long key = ~0ull;
+    if (p < c.n_particles) {
+      T x[3];
+      load_row(st, c.ld, p, 0, 3, x);
+      Stencil<T> s;
+      ok = make_stencil(c, x, s);  // out-of-grid particles are skipped (and flagged) by the scatter
+      if (ok) {
+        scene = pscene[p];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    lo[d] = s.base[d] >> 2;
-    hi[d] = (s.base[d] + 2) >> 2;
+        for (int d = 0; d < 3; ++d) {
+          lo[d] = s.base[d] >> 2;
+          ext[d] = ((s.base[d] + 2) >> 2) - lo[d];  // 0 or 1
+        }
+        // n_grid <= 1024: block coordinates fit 9 bits
+        key = ((unsigned long long)scene << 30) | ((unsigned long long)lo[0] << 21) |
+              ((unsigned long long)lo[1] << 12) | ((unsigned long long)lo[2] << 3) |
+              (unsigned long long)(ext[0] << 2 | ext[1] << 1 | ext[2]);
+      }
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (ok && lane == __ffs(peers) - 1) {
+      unsigned char* f = flags + (int64_t)scene * c.NB3;
+      const int nb = c.nb;
+      for (int bi = lo[0]; bi <= lo[0] + ext[0]; ++bi)
+        for (int bj = lo[1]; bj <= lo[1] + ext[1]; ++bj)
+          for (int bk = lo[2]; bk <= lo[2] + ext[2]; ++bk) f[((int64_t)bi * nb + bj) * nb + bk] = 1;
+    }
   }
-  unsigned char* f = flags + (int64_t)pscene[p] * c.NB3;
-  const int nb = c.nb;
-  for (int bi = lo[0]; bi <= hi[0]; ++bi)
-    for (int bj = lo[1]; bj <= hi[1]; ++bj)
-      for (int bk = lo[2]; bk <= hi[2]; ++bk) f[((int64_t)bi * nb + bj) * nb + bk] = 1;
 }
-// list of flagged blocks (warp-aggregated append; order is not significant)
-static __global__ void __launch_bounds__(256) k_compact_blocks(const unsigned char* __restrict__ flags, int64_t total,
-                                                               int* __restrict__ active, int* __restrict__ counter,
-                                                               const int64_t* __restrict__ saved) {
-  if (saved && *saved >= 0) return;
+
+// one thread: reserve room for n active blocks of substep `slot` in the grid
+// store (bump allocator); slot_start = -1 when the store is full (the adjoint
+// then recomputes)
+MPM_DI void store_reserve(const MpmGridStore& st, int slot, int n) {
+  const unsigned long long start = atomicAdd(st.bump, (unsigned long long)n);
+  const bool fits = start + (unsigned long long)n <= (unsigned long long)st.capacity;
+  st.slot_start[slot] = fits ? (int64_t)start : -1;
+  st.slot_count[slot] = fits ? n : 0;
+}
+
+// List of flagged blocks (warp-aggregated append; order is not significant).
+// The appending warp zeroes its blocks in grids a and b (either may be null).
+// With reserve_slot >= 0 the last CTA to finish (threadfence + ticket, no
+// waiting) reserves room for the list in the grid store.
+template <typename T>
+__global__ void __launch_bounds__(256) k_compact_clear(const unsigned char* __restrict__ flags, int64_t total,
+                                                       int* __restrict__ active, int* __restrict__ counter,
+                                                       unsigned* __restrict__ ticket, Node<T>* __restrict__ a,
+                                                       Node<T>* __restrict__ b, const int64_t* __restrict__ saved,
+                                                       MpmGridStore store, int reserve_slot) {
+  if (saved && *saved >= 0) return;  // list and grid a restored; b zeroed by the restore
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool f = i < total && flags[i] != 0;
-  const unsigned m = __ballot_sync(0xffffffffu, f);
-  if (m == 0) return;
+  unsigned m = __ballot_sync(0xffffffffu, f);
   const int lane = threadIdx.x & 31;
-  const int leader = __ffs(m) - 1;
-  int base = 0;
-  if (lane == leader) base = atomicAdd(counter, __popc(m));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  if (f) active[base + __popc(m & ((1u << lane) - 1u))] = (int)i;
-}
-// zero the listed blocks of one or two grids (a is kept when restored from the store)
-template <typename T>
-__global__ void __launch_bounds__(256) k_clear_blocks(const int* __restrict__ active, const int* __restrict__ n_active,
-                                                      Node<T>* __restrict__ a, Node<T>* __restrict__ b,
-                                                      const int64_t* __restrict__ saved) {
-  if (saved && *saved >= 0) a = nullptr;
-  if (!a && !b) return;
-  const int64_t n = (int64_t)(*n_active) * 64;
-  const Node<T> z = {T(0), T(0), T(0), T(0)};
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t idx = (int64_t)active[i >> 6] * 64 + (i & 63);
-    if (a) a[idx] = z;
-    if (b) b[idx] = z;
+  if (m) {
+    const int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (f) active[base + __popc(m & ((1u << lane) - 1u))] = (int)i;
+    const int64_t w0 = i - lane;
+    const Node<T> z = {T(0), T(0), T(0), T(0)};
+    while (m) {
+      const int k = __ffs(m) - 1;
+      m &= m - 1;
+      const int64_t node0 = (w0 + k) * 64;
+#pragma unroll
+      for (int l = 0; l < 64; l += 32) {
+        if (a) a[node0 + l + lane] = z;
+        if (b) b[node0 + l + lane] = z;
+      }
+    }
+  }
+  if (reserve_slot >= 0) {
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+      __threadfence();
+      store_reserve(store, reserve_slot, atomicAdd(counter, 0));
+    }
   }
 }
 
@@ -1184,15 +1246,6 @@ __global__ void __launch_bounds__(256) k_clear_blocks(const int* __restrict__ ac
 // grid store: the forward grid of a substep (its active blocks) is kept so
 // the adjoint substep restores it instead of recomputing p2g
 // ---------------------------------------------------------------------------
-// one thread: reserve room for this substep's active blocks (bump allocator);
-// slot_start = -1 when the store is full (the adjoint then recomputes)
-static __global__ void k_store_reserve(MpmGridStore st, int slot, const int* __restrict__ n_active) {
-  const int n = *n_active;
-  const unsigned long long start = atomicAdd(st.bump, (unsigned long long)n);
-  const bool fits = start + (unsigned long long)n <= (unsigned long long)st.capacity;
-  st.slot_start[slot] = fits ? (int64_t)start : -1;
-  st.slot_count[slot] = fits ? n : 0;
-}
 template <typename T>
 __global__ void __launch_bounds__(256) k_store_copy(MpmGridStore st, int slot, const int* __restrict__ active,
                                                     const Node<T>* __restrict__ grid) {
@@ -1206,20 +1259,24 @@ __global__ void __launch_bounds__(256) k_store_copy(MpmGridStore st, int slot, c
     if ((i & 63) == 0) st.block_ids[start + (i >> 6)] = blk;
   }
 }
-// restore the active list and the grid blocks of a stored substep
+// restore the active list and the grid blocks of a stored substep; the same
+// blocks of grid b (may be null) are zeroed
 template <typename T>
 __global__ void __launch_bounds__(256) k_store_restore(MpmGridStore st, int slot, int* __restrict__ active,
-                                                       int* __restrict__ n_active, Node<T>* __restrict__ grid) {
+                                                       int* __restrict__ n_active, Node<T>* __restrict__ grid,
+                                                       Node<T>* __restrict__ b) {
   const int64_t start = st.slot_start[slot];
   if (start < 0) return;
   const int cnt = st.slot_count[slot];
   if (blockIdx.x == 0 && threadIdx.x == 0) *n_active = cnt;
   const Node<T>* src = reinterpret_cast<const Node<T>*>(st.blocks);
+  const Node<T> z = {T(0), T(0), T(0), T(0)};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)cnt * 64;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int blk = st.block_ids[start + (i >> 6)];
     if ((i & 63) == 0) active[i >> 6] = blk;
     grid[(int64_t)blk * 64 + (i & 63)] = src[(start << 6) + i];
+    if (b) b[(int64_t)blk * 64 + (i & 63)] = z;
   }
 }
 
