@@ -861,11 +861,39 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 2) k_g2p_adj(Consts<
     for (int j = 0; j < 3; ++j) gC[3 * i + j] *= k4;
     ux[i] = gnv[i] - (gC[3 * i] * s.fx[0] + gC[3 * i + 1] * s.fx[1] + gC[3 * i + 2] * s.fx[2]);
   }
+  // weight adjoints g_wgt(o) = gv(o) . u(o): the 27 gathers of the grid
+  // velocity in one unrolled loop (their loads issue together), before the
+  // scatter, which then touches no global memory but its atomics
+  if (ok) {
+    T vx[3] = {ux[0], ux[1], ux[2]};
+#pragma unroll
+    for (int ox = 0; ox < 3; ++ox) {
+      T vy[3] = {vx[0], vx[1], vx[2]};
+#pragma unroll
+      for (int oy = 0; oy < 3; ++oy) {
+        T vz[3] = {vy[0], vy[1], vy[2]};
+#pragma unroll
+        for (int oz = 0; oz < 3; ++oz) {
+          const Node<T> n = g[A.at(ox, oy, oz)];
+          const T gv[3] = {n.x, n.y, n.z};
+          const T g_wgt = dot3(gv, vz);
+          gw[ox][0] += g_wgt * s.w[oy][1] * s.w[oz][2];
+          gw[oy][1] += g_wgt * s.w[ox][0] * s.w[oz][2];
+          gw[oz][2] += g_wgt * s.w[ox][0] * s.w[oy][1];
+#pragma unroll
+          for (int i = 0; i < 3; ++i) vz[i] += gC[3 * i + 2];
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i) vy[i] += gC[3 * i + 1];
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) vx[i] += gC[3 * i];
+    }
+  }
 #pragma unroll 1
   for (int ox = 0; ox < 3; ++ox) {
     const T wx = sel3(s.w[0][0], s.w[1][0], s.w[2][0], ox);
     const int ax = sel3(A.ax[0], A.ax[1], A.ax[2], ox);
-    T gwx = T(0);
     T uy[3] = {ux[0], ux[1], ux[2]};
 #pragma unroll
     for (int oy = 0; oy < 3; ++oy) {
@@ -876,21 +904,12 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 2) k_g2p_adj(Consts<
         T sc3[3] = {wgt * uz[0], wgt * uz[1], wgt * uz[2]};
         if constexpr (slab) {
           sb->v[lane][oy * 3 + oz] = make_float4(sc3[0], sc3[1], sc3[2], 0.f);
-        } else if (seg.steps) {
+        } else {
+          if (seg.steps) {
 #pragma unroll
-          for (int k = 0; k < 3; ++k) sc3[k] = seg_scan(sc3[k], seg);
-        }
-        if (ok) {
-          const int64_t a = ax + A.ay[oy] + A.az[oz];
-          if constexpr (!slab) {
-            if (seg.tail) atomic_add_node3(gg + a, sc3[0], sc3[1], sc3[2]);
+            for (int k = 0; k < 3; ++k) sc3[k] = seg_scan(sc3[k], seg);
           }
-          Node<T> n = g[a];
-          const T gv[3] = {n.x, n.y, n.z};
-          T g_wgt = dot3(gv, uz);
-          gwx += g_wgt * s.w[oy][1] * s.w[oz][2];
-          gw[oy][1] += g_wgt * wx * s.w[oz][2];
-          gw[oz][2] += g_wgt * wx * s.w[oy][1];
+          if (ok && seg.tail) atomic_add_node3(gg + ax + A.ay[oy] + A.az[oz], sc3[0], sc3[1], sc3[2]);
         }
 #pragma unroll
         for (int i = 0; i < 3; ++i) uz[i] += gC[3 * i + 2];
@@ -900,7 +919,6 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 2) k_g2p_adj(Consts<
     }
 #pragma unroll
     for (int i = 0; i < 3; ++i) ux[i] += gC[3 * i];
-    add3(gw[0][0], gw[1][0], gw[2][0], ox, gwx);
     if constexpr (slab) {
       sb->base[lane] = gg + ax;
       __syncwarp();
