@@ -34,6 +34,8 @@ struct MpmHandle {
   void* grid[4] = {nullptr, nullptr, nullptr, nullptr};
   unsigned char* d_blockbuf = nullptr;
   int* d_active = nullptr;
+  void* d_tools_t = nullptr;  // tools in the compute precision (converted by mpm_set_tools)
+  void* d_poses_t = nullptr;  // poses of the current substep in the compute precision
   int sm_count = 1;
   std::string err;
   int64_t launches = 0;
@@ -95,6 +97,7 @@ mpm::LaunchCtx ctx(MpmHandle* h, void* stream) {
   L.pscene = h->d_pscene;
   L.tools = h->d_tools;
   L.tool_off = h->d_tool_off;
+  L.n_tools = h->n_tools;
   L.status = h->d_status;
   L.grid_a = h->grid[0];
   L.grid_b = h->grid[1];
@@ -102,6 +105,8 @@ mpm::LaunchCtx ctx(MpmHandle* h, void* stream) {
   L.grid_d = h->grid[3];
   L.blockbuf = h->d_blockbuf;
   L.active = h->d_active;
+  L.tools_t = h->d_tools_t;
+  L.poses_t = h->d_poses_t;
   L.sm_count = h->sm_count;
   L.stream = (cudaStream_t)stream;
   L.launches = &h->launches;
@@ -215,6 +220,8 @@ int mpm_destroy(MpmHandle* h) {
   for (int i = 0; i < 4; ++i) cudaFree(h->grid[i]);
   cudaFree(h->d_blockbuf);
   cudaFree(h->d_active);
+  cudaFree(h->d_tools_t);
+  cudaFree(h->d_poses_t);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
   delete h;
   return MPM_OK;
@@ -271,16 +278,24 @@ int mpm_set_tools(MpmHandle* h, const MpmToolDesc* tools, int32_t n_tools) {
     ncols += (tools[i].type == MPM_TOOL_GRIPPER || tools[i].type == MPM_TOOL_GRIPPER2) ? 2 : 1;
   }
   cudaError_t e = cudaSuccess;
-  if (n_tools > h->n_tools) {
+  if (n_tools > h->n_tools || !h->d_tools_t) {
     cudaFree(h->d_tools);
     cudaFree(h->d_col_off);
+    cudaFree(h->d_tools_t);
+    cudaFree(h->d_poses_t);
     h->d_tools = nullptr;
     h->d_col_off = nullptr;
-    e = cudaMalloc(&h->d_tools, n_tools * sizeof(MpmToolDesc));
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_col_off, n_tools * sizeof(int));
+    h->d_tools_t = nullptr;
+    h->d_poses_t = nullptr;
+    e = cudaMalloc(&h->d_tools, std::max(n_tools, 1) * sizeof(MpmToolDesc));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_col_off, std::max(n_tools, 1) * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_tools_t, mpm::tools_t_bytes(n_tools));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_poses_t, mpm::poses_t_bytes(n_tools));
     if (e != cudaSuccess) return cuda_fail(h, e, "mpm_set_tools: cudaMalloc");
   }
   if (n_tools > 0) e = cudaMemcpy(h->d_tools, tools, n_tools * sizeof(MpmToolDesc), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = mpm::convert_tools(h->p.precision, n_tools, h->d_tools, h->d_tools_t, nullptr);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
   if (e == cudaSuccess && n_tools > 0)
     e = cudaMemcpy(h->d_col_off, coff.data(), n_tools * sizeof(int), cudaMemcpyHostToDevice);
   h->n_cols = ncols;

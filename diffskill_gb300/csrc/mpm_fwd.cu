@@ -44,10 +44,11 @@ static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs
 // this substep the list and grid a are restored from it and b is zeroed.
 // ``reserve`` (may be null): the forward's grid store; room for the list is
 // reserved in slot ``reserve_slot`` by the compaction's last CTA.
+// The compaction also fills L.tooltab for the poses pose_f, pose_f1.
 template <typename T>
 cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* b,
                            const MpmGridStore* restore, int restore_slot, const MpmGridStore* reserve,
-                           int reserve_slot) {
+                           int reserve_slot, const double* pose_f, const double* pose_f1) {
   const int64_t total = (int64_t)c.n_scenes * c.NB3;
   int* counter = reinterpret_cast<int*>(L.blockbuf);
   unsigned* ticket = reinterpret_cast<unsigned*>(L.blockbuf + 4);
@@ -63,14 +64,29 @@ cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, 
   }
   MpmGridStore rs{};
   if (reserve) rs = *reserve;
+  const PoseTableArgs tt{L.n_tools, pose_f, pose_f1, L.poses_t};
   MPM_LAUNCH(L, MPM_K_CLEAR, k_compact_clear<T>, blocks_for(total, 256), 256, flags, total, L.active, counter, ticket,
-             a, b, saved, rs, reserve ? reserve_slot : -1);
+             a, b, saved, rs, reserve ? reserve_slot : -1, tt);
   return cudaGetLastError();
 }
 template cudaError_t prepare_blocks<float>(const LaunchCtx&, const Consts<float>&, const float*, Node<float>*,
-                                           Node<float>*, const MpmGridStore*, int, const MpmGridStore*, int);
+                                           Node<float>*, const MpmGridStore*, int, const MpmGridStore*, int,
+                                           const double*, const double*);
 template cudaError_t prepare_blocks<double>(const LaunchCtx&, const Consts<double>&, const double*, Node<double>*,
-                                            Node<double>*, const MpmGridStore*, int, const MpmGridStore*, int);
+                                            Node<double>*, const MpmGridStore*, int, const MpmGridStore*, int,
+                                            const double*, const double*);
+
+size_t tools_t_bytes(int64_t n_tools) { return (size_t)(n_tools > 0 ? n_tools : 1) * sizeof(Tool<double>); }
+size_t poses_t_bytes(int64_t n_tools) { return (size_t)(n_tools > 0 ? n_tools : 1) * 16 * sizeof(double); }
+cudaError_t convert_tools(int precision, int n, const MpmToolDesc* tools, void* tools_t, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const unsigned g = blocks_for(n, 128);
+  if (precision == MPM_PREC_FP64)
+    k_tools_convert<double><<<g, 128, 0, s>>>(n, tools, (Tool<double>*)tools_t);
+  else
+    k_tools_convert<float><<<g, 128, 0, s>>>(n, tools, (Tool<float>*)tools_t);
+  return cudaGetLastError();
+}
 
 unsigned grid_blocks_launch(const LaunchCtx& L, int64_t total_blocks) {
   int64_t g = (int64_t)L.sm_count * 16;
@@ -84,7 +100,7 @@ cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const d
   Node<T>* gin = (Node<T>*)L.grid_a;
   Node<T>* gout = (Node<T>*)L.grid_b;
   const int* counter = reinterpret_cast<const int*>(L.blockbuf);
-  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, (Node<T>*)nullptr, nullptr, -1, store, slot);
+  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, (Node<T>*)nullptr, nullptr, -1, store, slot, pose_f, pose_f1);
   if (e != cudaSuccess) return e;
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S>), blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gin,
@@ -92,7 +108,7 @@ cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const d
   if (store)
     MPM_LAUNCH(L, MPM_K_CLEAR, k_store_copy<T>, (unsigned)(L.sm_count * 8), 256, *store, slot, L.active, gin);
   MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3), 64, c, L.active,
-             counter, gin, gout, L.tools, L.tool_off, pose_f, pose_f1);
+             counter, gin, gout, (const Tool<T>*)L.tools_t, (const T*)L.poses_t, L.tool_off);
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_G2P, k_g2p<T>, blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gout);
   return cudaGetLastError();

@@ -562,28 +562,48 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 6 : 
   }
 }
 
-// Per-CTA tool table of one scene in shared memory.
+// Tools in the compute precision, for grid_op and grid_op.grad.  The tool
+// fields (primive_base.py:313-329) are converted once when the tools are set
+// (k_tools_convert: tools_t[i] = Tool<T> of descriptor i).  The poses of
+// frames f and f+1 are converted every substep by the block compaction
+// (poses_t[16 i + k]: k < 8 frame f, else frame f+1, one value per thread).
+// Both kernels read them straight from global memory: the lanes of a warp
+// load the same words (a broadcast), with no per-block staging, barrier or
+// FP64 conversion.
 template <typename T>
-struct SceneTools {
-  int n;
-  Tool<T> tool[MAX_TOOLS_PER_SCENE];
-  Pose<T> p0[MAX_TOOLS_PER_SCENE], p1[MAX_TOOLS_PER_SCENE];
-};
-// loads the tools of `scene` (all threads call; one barrier inside)
-template <typename T>
-MPM_DI void load_scene_tools(SceneTools<T>& sh, int scene, const MpmToolDesc* __restrict__ tools,
-                             const int* __restrict__ tool_off, const double* __restrict__ pose_f,
-                             const double* __restrict__ pose_f1) {
-  int t0 = tool_off[scene], t1 = tool_off[scene + 1];
-  int n = t1 - t0;
-  if (threadIdx.x == 0) sh.n = n;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    to_tool(tools[t0 + i], sh.tool[i]);
-    to_pose(pose_f + 8 * (t0 + i), sh.p0[i]);
-    to_pose(pose_f1 + 8 * (t0 + i), sh.p1[i]);
-  }
-  __syncthreads();
+__global__ void __launch_bounds__(128) k_tools_convert(int n, const MpmToolDesc* __restrict__ tools,
+                                                       Tool<T>* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) to_tool(tools[i], out[i]);
 }
+struct PoseTableArgs {
+  int n_tools;
+  const double *pose_f, *pose_f1;
+  void* poses;  // T[n_tools * 16]
+};
+template <typename T>
+MPM_DI void pose_table_fill(const PoseTableArgs& a, int64_t i, int64_t stride) {
+  for (int64_t j = i; j < (int64_t)a.n_tools * 16; j += stride) {
+    const int64_t t = j >> 4;
+    const int k = (int)(j & 15);
+    static_cast<T*>(a.poses)[j] = T(k < 8 ? a.pose_f[8 * t + k] : a.pose_f1[8 * t + k - 8]);
+  }
+}
+// the tools of one scene: tool[t], pose p0(t) at frame f, p1(t) at frame f+1
+template <typename T>
+struct SceneToolView {
+  int n;
+  const Tool<T>* tool;
+  const Pose<T>* pose;
+  MPM_DI SceneToolView(const Tool<T>* tools_t, const T* poses_t, const int* tool_off, int scene) {
+    const int t0 = tool_off[scene];
+    n = tool_off[scene + 1] - t0;
+    tool = tools_t + t0;
+    pose = reinterpret_cast<const Pose<T>*>(poses_t + 16 * (int64_t)t0);
+  }
+  MPM_DI const Pose<T>& p0(int t) const { return pose[2 * t]; }
+  MPM_DI const Pose<T>& p1(int t) const { return pose[2 * t + 1]; }
+};
 
 // wall conditions of grid_op (mpm_simulator.py:241-260) with optional tape
 template <typename T>
@@ -660,33 +680,19 @@ MPM_DI void walls_vjp(const Consts<T>& c, const int* I, const WallTape<T>& tp, T
 }
 
 // Per-CTA tool table, reloaded when the block's scene changes.
-template <typename T>
-MPM_DI void scene_tools_for(SceneTools<T>& sh, int& cur, int scene, const MpmToolDesc* __restrict__ tools,
-                            const int* __restrict__ tool_off, const double* __restrict__ pose_f,
-                            const double* __restrict__ pose_f1) {
-  __syncthreads();  // the previous block is done with sh
-  if (scene != cur) {  // uniform: one block per CTA iteration
-    load_scene_tools(sh, scene, tools, tool_off, pose_f, pose_f1);
-    cur = scene;
-  }
-}
-
 // grid_op over the active blocks: one 64-thread CTA per block, grid-stride
 template <typename T>
 __global__ void __launch_bounds__(64) k_grid_op(Consts<T> c, const int* __restrict__ active,
                                                 const int* __restrict__ n_active,
                                                 const Node<T>* __restrict__ grid_in, Node<T>* __restrict__ grid_out,
-                                                const MpmToolDesc* __restrict__ tools,
-                                                const int* __restrict__ tool_off, const double* __restrict__ pose_f,
-                                                const double* __restrict__ pose_f1) {
-  __shared__ SceneTools<T> sh;
-  int cur = -1;
+                                                const Tool<T>* __restrict__ tools_t, const T* __restrict__ poses_t,
+                                                const int* __restrict__ tool_off) {
   const int na = *n_active;
   for (int b = blockIdx.x; b < na; b += gridDim.x) {
     const int64_t gb = active[b];
     int I[3];
     const int scene = block_node(c, gb, threadIdx.x, I);
-    scene_tools_for(sh, cur, scene, tools, tool_off, pose_f, pose_f1);
+    const SceneToolView<T> sh(tools_t, poses_t, tool_off, scene);
     const int64_t idx = gb * 64 + threadIdx.x;
     Node<T> in = grid_in[idx];
     Node<T> out = {T(0), T(0), T(0), in.w};
@@ -694,7 +700,7 @@ __global__ void __launch_bounds__(64) k_grid_op(Consts<T> c, const int* __restri
       T inv = T(1) / in.w;
       T v[3] = {inv * in.x + c.gdt[0], inv * in.y + c.gdt[1], inv * in.z + c.gdt[2]};
       const T p[3] = {T(I[0]) * c.dx, T(I[1]) * c.dx, T(I[2]) * c.dx};
-      for (int t = 0; t < sh.n; ++t) tool_collide(sh.tool[t], sh.p0[t], sh.p1[t], p, c.dt, v);
+      for (int t = 0; t < sh.n; ++t) tool_collide(sh.tool[t], sh.p0(t), sh.p1(t), p, c.dt, v);
       walls(c, I, v, (WallTape<T>*)nullptr);
       if (!(finite(v[0]) && finite(v[1]) && finite(v[2]))) atomicOr(c.status, MPM_STATUS_NONFINITE);
       out.x = v[0];
@@ -981,19 +987,15 @@ __global__ void __launch_bounds__(64) k_grid_op_adj(Consts<T> c, const int* __re
                                                     const int* __restrict__ n_active,
                                                     const Node<T>* __restrict__ grid_in,
                                                     const Node<T>* __restrict__ g_grid, Node<T>* __restrict__ g_in,
-                                                    const MpmToolDesc* __restrict__ tools,
-                                                    const int* __restrict__ tool_off,
-                                                    const double* __restrict__ pose_f,
-                                                    const double* __restrict__ pose_f1,
+                                                    const Tool<T>* __restrict__ tools_t,
+                                                    const T* __restrict__ poses_t, const int* __restrict__ tool_off,
                                                     double* __restrict__ g_pose_f, double* __restrict__ g_pose_f1) {
-  __shared__ SceneTools<T> sh;
-  int cur = -1;
   const int na = *n_active;
   for (int b = blockIdx.x; b < na; b += gridDim.x) {
     const int64_t gb = active[b];
     int I[3];
     const int scene = block_node(c, gb, threadIdx.x, I);
-    scene_tools_for(sh, cur, scene, tools, tool_off, pose_f, pose_f1);
+    const SceneToolView<T> sh(tools_t, poses_t, tool_off, scene);
     const int64_t idx = gb * 64 + threadIdx.x;
     Node<T> in = grid_in[idx];
     Node<T> go = g_grid[idx];
@@ -1008,7 +1010,7 @@ __global__ void __launch_bounds__(64) k_grid_op_adj(Consts<T> c, const int* __re
       for (int t = 0; t < sh.n; ++t) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) vt[t][k] = v[k];
-        tool_collide(sh.tool[t], sh.p0[t], sh.p1[t], p, c.dt, v);
+        tool_collide(sh.tool[t], sh.p0(t), sh.p1(t), p, c.dt, v);
       }
       walls(c, I, v, &wt);
       walls_vjp(c, I, wt, g);
@@ -1018,7 +1020,7 @@ __global__ void __launch_bounds__(64) k_grid_op_adj(Consts<T> c, const int* __re
       PoseGrad<T> g0, g1;
       g0.zero();
       g1.zero();
-      if (active_node) tool_collide_vjp(sh.tool[t], sh.p0[t], sh.p1[t], p, c.dt, vt[t], g, g0, g1);
+      if (active_node) tool_collide_vjp(sh.tool[t], sh.p0(t), sh.p1(t), p, c.dt, vt[t], g, g0, g1);
       if (__any_sync(0xffffffffu, active_node)) {
         double* d0 = g_pose_f + 8 * (t0 + t);
         double* d1 = g_pose_f1 + 8 * (t0 + t);
@@ -1214,15 +1216,17 @@ MPM_DI void store_reserve(const MpmGridStore& st, int slot, int n) {
 // List of flagged blocks (warp-aggregated append; order is not significant).
 // The appending warp zeroes its blocks in grids a and b (either may be null).
 // With reserve_slot >= 0 the last CTA to finish (threadfence + ticket, no
-// waiting) reserves room for the list in the grid store.
+// waiting) reserves room for the list in the grid store.  The threads also
+// convert the substep's tool poses (pose_table_fill).
 template <typename T>
 __global__ void __launch_bounds__(256) k_compact_clear(const unsigned char* __restrict__ flags, int64_t total,
                                                        int* __restrict__ active, int* __restrict__ counter,
                                                        unsigned* __restrict__ ticket, Node<T>* __restrict__ a,
                                                        Node<T>* __restrict__ b, const int64_t* __restrict__ saved,
-                                                       MpmGridStore store, int reserve_slot) {
-  if (saved && *saved >= 0) return;  // list and grid a restored; b zeroed by the restore
+                                                       MpmGridStore store, int reserve_slot, PoseTableArgs pt) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  pose_table_fill<T>(pt, i, (int64_t)gridDim.x * blockDim.x);
+  if (saved && *saved >= 0) return;  // list and grid a restored; b zeroed by the restore
   const bool f = i < total && flags[i] != 0;
   unsigned m = __ballot_sync(0xffffffffu, f);
   const int lane = threadIdx.x & 31;

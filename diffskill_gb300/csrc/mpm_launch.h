@@ -35,6 +35,7 @@ struct LaunchCtx {
   const int* pscene;           // [n_particles] scene of each particle
   const MpmToolDesc* tools;    // [n_tools] device
   const int* tool_off;         // [n_scenes + 1] device
+  int n_tools;
   unsigned int* status;        // sticky status word
   void* grid_a;                // scratch grids, n_scenes*G nodes of 4 reals
   void* grid_b;                //   (block-contiguous layout, see mpm_kernels.cuh)
@@ -42,6 +43,8 @@ struct LaunchCtx {
   void* grid_d;
   unsigned char* blockbuf;     // [16-byte counter header][n_scenes * NB3 block flags]
   int* active;                 // [n_scenes * NB3] list of active blocks
+  const void* tools_t;         // [n_tools] Tool<T>, converted when the tools are set (convert_tools)
+  void* poses_t;               // [n_tools * 16] T: poses of frames f, f+1, converted every substep
   int sm_count;                // multiprocessors of the device (grid-stride launch sizes)
   cudaStream_t stream;
   int64_t* launches;           // launch counter
@@ -63,6 +66,13 @@ struct LaunchCtx {
     prof_end((L).prof, _slot, MPM_K_CLEAR, (L).stream);                \
     if (_e != cudaSuccess) return _e;                                  \
   } while (0)
+
+// bytes of the converted tools and of the per-substep pose table (the
+// double-precision sizes cover both precisions)
+size_t tools_t_bytes(int64_t n_tools);
+size_t poses_t_bytes(int64_t n_tools);
+// converts n tool descriptors into Tool<T> of the handle's precision
+cudaError_t convert_tools(int precision, int n, const MpmToolDesc* tools, void* tools_t, cudaStream_t s);
 
 // bytes of the block-flag buffer (counter header + one flag per block)
 inline size_t blockbuf_bytes(int64_t n_scenes, int n_grid) {

@@ -37,10 +37,14 @@ namespace {
 //   [256, 256 + 8*tool size)    tool table
 //   [4096, 4096 + 16 + 8000)    active-block counter and flags (<= 20^3 blocks)
 //   [16384, 16384 + 32000)      active-block list
+//   [49152, +8 Tool<double>)    the tools in the compute precision
+//   [kPosesT, +8*16 doubles)     their poses at frames f, f+1 in the compute precision
 //   [kHeader, +kScene)          zero scene index of every particle
 //   [kHeader+kScene, +kGrids)   forward grid (mv, m) then velocity grid
 constexpr size_t kBlockBuf = 4096;
 constexpr size_t kActive = 16384;
+constexpr size_t kToolsT = 49152;
+constexpr size_t kPosesT = kToolsT + 8 * sizeof(mpm::Tool<double>);
 constexpr int64_t kMaxBlocks = 8000;  // (80/4)^3
 constexpr size_t kHeader = 65536;
 constexpr int64_t kMaxParticles = int64_t(1) << 20;             // 1,048,576 particles
@@ -48,7 +52,8 @@ constexpr size_t kScene = size_t(kMaxParticles) * sizeof(int);  // 4 MiB
 constexpr size_t kGrids = size_t(16) << 20;                     // 16 MiB for the two grids
 constexpr size_t kScratchBytes = kHeader + kScene + kGrids;     // 20 MiB + 64 KiB
 static_assert(kBlockBuf + 16 + kMaxBlocks <= kActive, "block flags overlap the list");
-static_assert(kActive + kMaxBlocks * sizeof(int) <= kHeader, "block list overlaps the scene index");
+static_assert(kActive + kMaxBlocks * sizeof(int) <= kToolsT, "block list overlaps the tool table");
+static_assert(kPosesT + 8 * 16 * sizeof(double) <= kHeader, "pose table overlaps the scene index");
 
 static __device__ __align__(256) unsigned char g_static_scratch[kScratchBytes];
 
@@ -141,6 +146,8 @@ int mpm_substep_fwd_static(const MpmParams* params, const MpmToolDesc* tools, in
   if (e == cudaSuccess) e = cudaMemcpyAsync(base + 16, toff, sizeof(toff), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && n_tools > 0)
     e = cudaMemcpyAsync(base + 256, tools, size_t(n_tools) * sizeof(MpmToolDesc), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = mpm::convert_tools(p.precision, n_tools, reinterpret_cast<const MpmToolDesc*>(base + 256), base + kToolsT, s);
   if (e != cudaSuccess) return set_err(MPM_E_CUDA, std::string("mpm_substep_fwd_static: ") + cudaGetErrorString(e));
 
   int64_t launches = 0;
@@ -150,6 +157,7 @@ int mpm_substep_fwd_static(const MpmParams* params, const MpmToolDesc* tools, in
   L.pscene = reinterpret_cast<const int*>(base + kHeader);
   L.tools = reinterpret_cast<const MpmToolDesc*>(base + 256);
   L.tool_off = reinterpret_cast<const int*>(base + 16);
+  L.n_tools = n_tools;
   L.status = reinterpret_cast<unsigned int*>(base);
   L.grid_a = base + kHeader + kScene;              // active blocks cleared by the launcher before the scatter
   L.grid_b = base + kHeader + kScene + grid_bytes;  // fully written by grid_op
@@ -157,6 +165,8 @@ int mpm_substep_fwd_static(const MpmParams* params, const MpmToolDesc* tools, in
   L.grid_d = nullptr;
   L.blockbuf = base + kBlockBuf;  // cleared by the launcher every call
   L.active = reinterpret_cast<int*>(base + kActive);
+  L.tools_t = base + kToolsT;
+  L.poses_t = base + kPosesT;
   int sm = 1;
   if (cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sm < 1) sm = 1;
   L.sm_count = sm;
