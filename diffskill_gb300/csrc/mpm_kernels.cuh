@@ -72,6 +72,9 @@ MPM_DI void atomic_add_node3(Node<double>* n, double a, double b, double c) {
   atomicAdd(&n->z, c);
 }
 
+// L2 prefetch of the line holding p (no register, no wait)
+MPM_DI void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 // quadratic B-spline stencil (mpm_simulator.py:201-204); base truncates like
 // ti.cast(int)
 template <typename T>
@@ -1051,6 +1054,12 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 4 : 
                                                  const Node<T>* __restrict__ g_in) {
   int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= c.n_particles) return;
+  // the adjoint rows read after the forward recompute and the gather are
+  // fetched into L2 now, so those later loads do not wait on DRAM
+#pragma unroll
+  for (int k = 0; k < 3; ++k) prefetch_l2(g0 + (int64_t)k * c.ld + p);
+#pragma unroll
+  for (int k = 15; k < 24; ++k) prefetch_l2(g1 + (int64_t)k * c.ld + p);
   T x[3], v[3];
   S C[9], F[9];
   load_row(st, c.ld, p, 0, 3, x);
