@@ -1166,9 +1166,9 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 4 : 
 // active-block bookkeeping
 // ---------------------------------------------------------------------------
 // flags[scene*NB3 + block] = 1 for every block a particle stencil touches.
-// In cell order neighbouring particles touch the same blocks, so the lanes of
-// a warp with equal (scene, block range) elect one writer (__match_any_sync):
-// about one flag store per block per warp instead of one per particle.
+// In cell order neighbouring particles touch the same blocks, so a lane whose
+// (scene, block range) equals the previous lane's writes nothing: about one
+// flag store per block per warp instead of one per particle.
 // Grid-stride over warp-aligned ranges (the early exit of a restored substep
 // then costs a small grid).
 template <typename T>
@@ -1201,8 +1201,8 @@ __global__ void __launch_bounds__(256) k_mark_blocks(Consts<T> c, const T* __res
               (unsigned long long)(ext[0] << 2 | ext[1] << 1 | ext[2]);
       }
     }
-    const unsigned peers = __match_any_sync(0xffffffffu, key);
-    if (ok && lane == __ffs(peers) - 1) {
+    const unsigned long long prev = __shfl_up_sync(0xffffffffu, key, 1);
+    if (ok && (lane == 0 || prev != key)) {
       unsigned char* f = flags + (int64_t)scene * c.NB3;
       const int nb = c.nb;
       for (int bi = lo[0]; bi <= lo[0] + ext[0]; ++bi)
