@@ -34,6 +34,7 @@ struct MpmHandle {
   void* grid[4] = {nullptr, nullptr, nullptr, nullptr};
   unsigned char* d_blockbuf = nullptr;
   int* d_active = nullptr;
+  unsigned char* d_contact = nullptr;  // per active-list block: touched by a tool (adjoint)
   void* d_tools_t = nullptr;  // tools in the compute precision (converted by mpm_set_tools)
   void* d_poses_t = nullptr;  // poses of the current substep in the compute precision
   int sm_count = 1;
@@ -105,6 +106,7 @@ mpm::LaunchCtx ctx(MpmHandle* h, void* stream) {
   L.grid_d = h->grid[3];
   L.blockbuf = h->d_blockbuf;
   L.active = h->d_active;
+  L.contact = h->d_contact;
   L.tools_t = h->d_tools_t;
   L.poses_t = h->d_poses_t;
   L.sm_count = h->sm_count;
@@ -187,6 +189,7 @@ int mpm_create(const MpmParams* params, const int64_t* scene_offsets, MpmHandle*
   const int64_t nblocks = (int64_t)p.n_scenes * nb * nb * nb;
   ok = ok && cudaMalloc(&h->d_blockbuf, mpm::blockbuf_bytes(p.n_scenes, p.n_grid)) == cudaSuccess;
   ok = ok && cudaMalloc(&h->d_active, nblocks * sizeof(int)) == cudaSuccess;
+  ok = ok && cudaMalloc(&h->d_contact, nblocks) == cudaSuccess;
   if (ok) cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
   if (h->sm_count < 1) h->sm_count = 1;
   if (!ok) {
@@ -220,6 +223,7 @@ int mpm_destroy(MpmHandle* h) {
   for (int i = 0; i < 4; ++i) cudaFree(h->grid[i]);
   cudaFree(h->d_blockbuf);
   cudaFree(h->d_active);
+  cudaFree(h->d_contact);
   cudaFree(h->d_tools_t);
   cudaFree(h->d_poses_t);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);

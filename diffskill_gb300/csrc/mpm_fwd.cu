@@ -108,7 +108,8 @@ cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const d
   if (store)
     MPM_LAUNCH(L, MPM_K_CLEAR, k_store_copy<T>, (unsigned)(L.sm_count * 8), 256, *store, slot, L.active, gin);
   MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3), 64, c, L.active,
-             counter, gin, gout, (const Tool<T>*)L.tools_t, (const T*)L.poses_t, L.tool_off);
+             counter, gin, gout, (const Tool<T>*)L.tools_t, (const T*)L.poses_t, L.tool_off,
+             (unsigned char*)nullptr);
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_G2P, k_g2p<T>, blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gout);
   return cudaGetLastError();

@@ -598,9 +598,10 @@ struct SceneToolView {
   int n;
   const Tool<T>* tool;
   const Pose<T>* pose;
-  MPM_DI SceneToolView(const Tool<T>* tools_t, const T* poses_t, const int* tool_off, int scene) {
+  // none: a block no tool touches (the adjoint's light path: no tool terms)
+  MPM_DI SceneToolView(const Tool<T>* tools_t, const T* poses_t, const int* tool_off, int scene, bool none = false) {
     const int t0 = tool_off[scene];
-    n = tool_off[scene + 1] - t0;
+    n = none ? 0 : tool_off[scene + 1] - t0;
     tool = tools_t + t0;
     pose = reinterpret_cast<const Pose<T>*>(poses_t + 16 * (int64_t)t0);
   }
@@ -683,13 +684,16 @@ MPM_DI void walls_vjp(const Consts<T>& c, const int* I, const WallTape<T>& tp, T
 }
 
 // Per-CTA tool table, reloaded when the block's scene changes.
-// grid_op over the active blocks: one 64-thread CTA per block, grid-stride
+// grid_op over the active blocks: one 64-thread CTA per block, grid-stride.
+// contact (may be null): contact[b] = 1 when a tool's contact response was
+// applied to a node of list block b (read by grid_op.grad)
 template <typename T>
 __global__ void __launch_bounds__(64) k_grid_op(Consts<T> c, const int* __restrict__ active,
                                                 const int* __restrict__ n_active,
                                                 const Node<T>* __restrict__ grid_in, Node<T>* __restrict__ grid_out,
                                                 const Tool<T>* __restrict__ tools_t, const T* __restrict__ poses_t,
-                                                const int* __restrict__ tool_off) {
+                                                const int* __restrict__ tool_off,
+                                                unsigned char* __restrict__ contact) {
   const int na = *n_active;
   for (int b = blockIdx.x; b < na; b += gridDim.x) {
     const int64_t gb = active[b];
@@ -699,11 +703,12 @@ __global__ void __launch_bounds__(64) k_grid_op(Consts<T> c, const int* __restri
     const int64_t idx = gb * 64 + threadIdx.x;
     Node<T> in = grid_in[idx];
     Node<T> out = {T(0), T(0), T(0), in.w};
+    bool hit = false;
     if (in.w > T(1e-12)) {
       T inv = T(1) / in.w;
       T v[3] = {inv * in.x + c.gdt[0], inv * in.y + c.gdt[1], inv * in.z + c.gdt[2]};
       const T p[3] = {T(I[0]) * c.dx, T(I[1]) * c.dx, T(I[2]) * c.dx};
-      for (int t = 0; t < sh.n; ++t) tool_collide(sh.tool[t], sh.p0(t), sh.p1(t), p, c.dt, v);
+      for (int t = 0; t < sh.n; ++t) hit = tool_collide(sh.tool[t], sh.p0(t), sh.p1(t), p, c.dt, v) || hit;
       walls(c, I, v, (WallTape<T>*)nullptr);
       if (!(finite(v[0]) && finite(v[1]) && finite(v[2]))) atomicOr(c.status, MPM_STATUS_NONFINITE);
       out.x = v[0];
@@ -711,6 +716,10 @@ __global__ void __launch_bounds__(64) k_grid_op(Consts<T> c, const int* __restri
       out.z = v[2];
     }
     grid_out[idx] = out;
+    if (contact) {  // uniform: the adjoint's recompute records the blocks a tool touches
+      const int any = __syncthreads_or(hit);
+      if (threadIdx.x == 0) contact[b] = (unsigned char)(any != 0);
+    }
   }
 }
 
@@ -992,13 +1001,16 @@ __global__ void __launch_bounds__(64) k_grid_op_adj(Consts<T> c, const int* __re
                                                     const Node<T>* __restrict__ g_grid, Node<T>* __restrict__ g_in,
                                                     const Tool<T>* __restrict__ tools_t,
                                                     const T* __restrict__ poses_t, const int* __restrict__ tool_off,
+                                                    const unsigned char* __restrict__ contact,
                                                     double* __restrict__ g_pose_f, double* __restrict__ g_pose_f1) {
   const int na = *n_active;
   for (int b = blockIdx.x; b < na; b += gridDim.x) {
     const int64_t gb = active[b];
     int I[3];
     const int scene = block_node(c, gb, threadIdx.x, I);
-    const SceneToolView<T> sh(tools_t, poses_t, tool_off, scene);
+    // a block no tool touched in the recompute takes no tool term: its
+    // adjoint passes through the tools unchanged, with zero pose gradients
+    const SceneToolView<T> sh(tools_t, poses_t, tool_off, scene, contact && !contact[b]);
     const int64_t idx = gb * 64 + threadIdx.x;
     Node<T> in = grid_in[idx];
     Node<T> go = g_grid[idx];

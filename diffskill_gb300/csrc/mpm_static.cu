@@ -165,6 +165,7 @@ int mpm_substep_fwd_static(const MpmParams* params, const MpmToolDesc* tools, in
   L.grid_d = nullptr;
   L.blockbuf = base + kBlockBuf;  // cleared by the launcher every call
   L.active = reinterpret_cast<int*>(base + kActive);
+  L.contact = nullptr;  // forward only
   L.tools_t = base + kToolsT;
   L.poses_t = base + kPosesT;
   int sm = 1;

@@ -711,25 +711,29 @@ MPM_DI void finger_pos_vjp(const Pose<T>& P, T flag, const T* gfpos, PoseGrad<T>
 }
 
 // grid_op's call of primitives[i].collide (mpm_simulator.py:237-239)
+// returns whether the contact response was applied (else v passes unchanged,
+// and so does its adjoint, with zero pose gradients)
 template <typename T>
-MPM_DI void tool_collide(const Tool<T>& t, const Pose<T>& P0, const Pose<T>& P1, const T* p, T dt, T* v) {
+MPM_DI bool tool_collide(const Tool<T>& t, const Pose<T>& P0, const Pose<T>& P1, const T* p, T dt, T* v) {
   T out[3];
   if (fingered(t.type)) {
+    bool hit = false;
 #pragma unroll
     for (int side = 0; side < 2; ++side) {
       T flag = side == 0 ? T(-1) : T(1);
       T f0[3], f1[3];
       finger_pos(P0, flag, f0);
       finger_pos(P1, flag, f1);
-      collide_fwd(t, f0, P0.rot, T(0), f1, P1.rot, p, dt, v, out);
+      hit = collide_fwd(t, f0, P0.rot, T(0), f1, P1.rot, p, dt, v, out) || hit;
 #pragma unroll
       for (int k = 0; k < 3; ++k) v[k] = out[k];
     }
-    return;
+    return hit;
   }
-  collide_fwd(t, P0.pos, P0.rot, P0.gap, P1.pos, P1.rot, p, dt, v, out);
+  const bool hit = collide_fwd(t, P0.pos, P0.rot, P0.gap, P1.pos, P1.rot, p, dt, v, out);
 #pragma unroll
   for (int k = 0; k < 3; ++k) v[k] = out[k];
+  return hit;
 }
 // g: in = d/d vout, out = d/d vin
 template <typename T>
