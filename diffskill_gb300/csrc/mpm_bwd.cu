@@ -40,7 +40,7 @@ cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* st1, c
   const Tool<T>* tools_t = (const Tool<T>*)L.tools_t;
   const T* poses_t = (const T*)L.poses_t;
   MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, gb, 64, c, L.active, counter, gin, gout, tools_t, poses_t, L.tool_off,
-             L.contact);
+             L.contact, MpmGridStore{}, -1);
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_G2P_ADJ, k_g2p_adj<T>, pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
   MPM_LAUNCH(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, gb, 64, c, L.active, counter, gin, g_gout, g_gin, tools_t,

@@ -188,6 +188,8 @@ int mpm_create(const MpmParams* params, const int64_t* scene_offsets, MpmHandle*
   const int64_t nb = p.n_grid / 4;
   const int64_t nblocks = (int64_t)p.n_scenes * nb * nb * nb;
   ok = ok && cudaMalloc(&h->d_blockbuf, mpm::blockbuf_bytes(p.n_scenes, p.n_grid)) == cudaSuccess;
+  // block flags start clean; every compaction clears the flags it reads
+  ok = ok && cudaMemset(h->d_blockbuf, 0, mpm::blockbuf_bytes(p.n_scenes, p.n_grid)) == cudaSuccess;
   ok = ok && cudaMalloc(&h->d_active, nblocks * sizeof(int)) == cudaSuccess;
   ok = ok && cudaMalloc(&h->d_contact, nblocks) == cudaSuccess;
   if (ok) cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);

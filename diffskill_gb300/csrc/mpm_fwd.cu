@@ -37,14 +37,15 @@ template Consts<double> make_consts<double>(const LaunchCtx&);
 
 static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
-// Active blocks of frame st: clear flags, mark, then compact the list and
-// zero the listed blocks of grid a (and b if given).  Leaves the list in
-// L.active and its length at L.blockbuf[0..3] (a ticket counter at [4..7]).
+// Active blocks of frame st: mark, then compact the list and zero the listed
+// blocks of grid a (and b if given).  Leaves the list in L.active and its
+// length at L.blockbuf[0..3] (a ticket counter at [4..7]); the block flags at
+// L.blockbuf + 16 are clean before and after (cleared by the compaction).
 // ``restore`` (may be null): the adjoint's grid store; when its slot holds
 // this substep the list and grid a are restored from it and b is zeroed.
 // ``reserve`` (may be null): the forward's grid store; room for the list is
 // reserved in slot ``reserve_slot`` by the compaction's last CTA.
-// The compaction also fills L.tooltab for the poses pose_f, pose_f1.
+// The compaction also fills L.poses_t for the poses pose_f, pose_f1.
 template <typename T>
 cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* b,
                            const MpmGridStore* restore, int restore_slot, const MpmGridStore* reserve,
@@ -54,14 +55,13 @@ cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, 
   unsigned* ticket = reinterpret_cast<unsigned*>(L.blockbuf + 4);
   unsigned char* flags = L.blockbuf + 16;
   const int64_t* saved = restore ? restore->slot_start + restore_slot : nullptr;
-  MPM_MEMSET(L, L.blockbuf, blockbuf_bytes(c.n_scenes, c.n_grid));
-  if (restore)
-    MPM_LAUNCH(L, MPM_K_CLEAR, k_store_restore<T>, (unsigned)(L.sm_count * 8), 256, *restore, restore_slot,
-               L.active, counter, a, b);
-  if (c.n_particles > 0) {
-    const unsigned mb = blocks_for(c.n_particles, 256), cap = (unsigned)(L.sm_count * 16);
-    MPM_LAUNCH(L, MPM_K_CLEAR, k_mark_blocks<T>, mb < cap ? mb : cap, 256, c, st, L.pscene, flags, saved);
-  }
+  const unsigned cap = (unsigned)(L.sm_count * 16);
+  unsigned mb = blocks_for(c.n_particles, 256);
+  mb = restore ? cap : (mb < cap ? (mb > 0 ? mb : 1) : cap);
+  MpmGridStore rst{};
+  if (restore) rst = *restore;
+  MPM_LAUNCH(L, MPM_K_CLEAR, k_mark_or_restore<T>, mb, 256, c, st, L.pscene, flags, counter, rst,
+             restore ? restore_slot : -1, L.active, a, b);
   MpmGridStore rs{};
   if (reserve) rs = *reserve;
   const PoseTableArgs tt{L.n_tools, pose_f, pose_f1, L.poses_t};
@@ -105,11 +105,9 @@ cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const d
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S>), blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gin,
                (const int64_t*)nullptr);
-  if (store)
-    MPM_LAUNCH(L, MPM_K_CLEAR, k_store_copy<T>, (unsigned)(L.sm_count * 8), 256, *store, slot, L.active, gin);
   MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3), 64, c, L.active,
              counter, gin, gout, (const Tool<T>*)L.tools_t, (const T*)L.poses_t, L.tool_off,
-             (unsigned char*)nullptr);
+             (unsigned char*)nullptr, store ? *store : MpmGridStore{}, store ? slot : -1);
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_G2P, k_g2p<T>, blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gout);
   return cudaGetLastError();

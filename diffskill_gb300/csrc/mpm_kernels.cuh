@@ -16,9 +16,9 @@
 //
 // Sparse grid: the scratch grids of a substep are stored block-contiguous
 // (blocks of 4x4x4 nodes, 64 nodes = 1 KiB in FP32 per block).  Each substep
-// marks the blocks that particle stencils touch (k_mark_blocks), compacts them
-// into a device-side list and clears only those (k_compact_clear), and runs
-// grid_op / grid_op.grad over that list with
+// marks the blocks that particle stencils touch (k_mark_or_restore), compacts
+// them into a device-side list and clears only those (k_compact_clear), and
+// runs grid_op / grid_op.grad over that list with
 // grid-stride loops (no host round trip; capturable in a CUDA graph).  Nodes
 // outside the list hold no mass, so grid_op leaves them at zero exactly as the
 // dense reference does; g2p and p2g.grad only read nodes inside the list.
@@ -686,15 +686,19 @@ MPM_DI void walls_vjp(const Consts<T>& c, const int* I, const WallTape<T>& tp, T
 // Per-CTA tool table, reloaded when the block's scene changes.
 // grid_op over the active blocks: one 64-thread CTA per block, grid-stride.
 // contact (may be null): contact[b] = 1 when a tool's contact response was
-// applied to a node of list block b (read by grid_op.grad)
+// applied to a node of list block b (read by grid_op.grad).
+// store_slot >= 0: list block b of grid_in is also copied to the grid store
+// at slot_start + b (reserved by the compaction; -1 when the store is full)
 template <typename T>
 __global__ void __launch_bounds__(64) k_grid_op(Consts<T> c, const int* __restrict__ active,
                                                 const int* __restrict__ n_active,
                                                 const Node<T>* __restrict__ grid_in, Node<T>* __restrict__ grid_out,
                                                 const Tool<T>* __restrict__ tools_t, const T* __restrict__ poses_t,
                                                 const int* __restrict__ tool_off,
-                                                unsigned char* __restrict__ contact) {
+                                                unsigned char* __restrict__ contact, MpmGridStore store,
+                                                int store_slot) {
   const int na = *n_active;
+  const int64_t start = store_slot >= 0 ? store.slot_start[store_slot] : -1;
   for (int b = blockIdx.x; b < na; b += gridDim.x) {
     const int64_t gb = active[b];
     int I[3];
@@ -702,6 +706,10 @@ __global__ void __launch_bounds__(64) k_grid_op(Consts<T> c, const int* __restri
     const SceneToolView<T> sh(tools_t, poses_t, tool_off, scene);
     const int64_t idx = gb * 64 + threadIdx.x;
     Node<T> in = grid_in[idx];
+    if (start >= 0) {
+      reinterpret_cast<Node<T>*>(store.blocks)[((start + b) << 6) + threadIdx.x] = in;
+      if (threadIdx.x == 0) store.block_ids[start + b] = (int)gb;
+    }
     Node<T> out = {T(0), T(0), T(0), in.w};
     bool hit = false;
     if (in.w > T(1e-12)) {
@@ -1177,20 +1185,43 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 4 : 
 // ---------------------------------------------------------------------------
 // active-block bookkeeping
 // ---------------------------------------------------------------------------
-// flags[scene*NB3 + block] = 1 for every block a particle stencil touches.
-// In cell order neighbouring particles touch the same blocks, so a lane whose
-// (scene, block range) equals the previous lane's writes nothing: about one
-// flag store per block per warp instead of one per particle.
-// Grid-stride over warp-aligned ranges (the early exit of a restored substep
-// then costs a small grid).
+// Start of a substep's block bookkeeping, one launch:
+// - restore (when the grid store's slot holds this substep): the active list,
+//   its length and grid a come back from the store, and the same blocks of
+//   grid b (may be null) are zeroed;
+// - otherwise: the list length and the reservation ticket are reset, and
+//   flags[scene*NB3 + block] = 1 for every block a particle stencil touches.
+//   The flags are clean on entry (the compaction clears every flag it reads).
+//   In cell order neighbouring particles touch the same blocks, so a lane
+//   whose (scene, block range) equals the previous lane's writes nothing:
+//   about one flag store per block per warp instead of one per particle.
+// Grid-stride over warp-aligned ranges.
 template <typename T>
-__global__ void __launch_bounds__(256) k_mark_blocks(Consts<T> c, const T* __restrict__ st,
-                                                     const int* __restrict__ pscene,
-                                                     unsigned char* __restrict__ flags,
-                                                     const int64_t* __restrict__ saved) {
-  if (saved && *saved >= 0) return;
-  const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(256) k_mark_or_restore(Consts<T> c, const T* __restrict__ st,
+                                                         const int* __restrict__ pscene,
+                                                         unsigned char* __restrict__ flags, int* __restrict__ header,
+                                                         MpmGridStore store, int slot, int* __restrict__ active,
+                                                         Node<T>* __restrict__ a, Node<T>* __restrict__ b) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t start = slot >= 0 ? store.slot_start[slot] : -1;
+  if (start >= 0) {
+    const int cnt = store.slot_count[slot];
+    if (blockIdx.x == 0 && threadIdx.x == 0) header[0] = cnt;
+    const Node<T>* src = reinterpret_cast<const Node<T>*>(store.blocks);
+    const Node<T> z = {T(0), T(0), T(0), T(0)};
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)cnt * 64; i += stride) {
+      const int blk = store.block_ids[start + (i >> 6)];
+      if ((i & 63) == 0) active[i >> 6] = blk;
+      a[(int64_t)blk * 64 + (i & 63)] = src[(start << 6) + i];
+      if (b) b[(int64_t)blk * 64 + (i & 63)] = z;
+    }
+    return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    header[0] = 0;  // list length (the compaction's append counter)
+    header[1] = 0;  // reservation ticket
+  }
+  const int lane = threadIdx.x & 31;
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p - lane < c.n_particles; p += stride) {
     bool ok = false;
     int scene = 0, lo[3] = {0, 0, 0}, ext[3] = {0, 0, 0};
@@ -1224,9 +1255,11 @@ __global__ void __launch_bounds__(256) k_mark_blocks(Consts<T> c, const T* __res
   }
 }
 
-// one thread: reserve room for n active blocks of substep `slot` in the grid
-// store (bump allocator); slot_start = -1 when the store is full (the adjoint
-// then recomputes)
+// Grid store: the forward grid of a substep (its active blocks) is kept so the
+// adjoint substep restores it instead of recomputing p2g (copy in k_grid_op,
+// restore in k_mark_or_restore).  One thread reserves room for n active blocks
+// of substep `slot` (bump allocator); slot_start = -1 when the store is full
+// (the adjoint then recomputes)
 MPM_DI void store_reserve(const MpmGridStore& st, int slot, int n) {
   const unsigned long long start = atomicAdd(st.bump, (unsigned long long)n);
   const bool fits = start + (unsigned long long)n <= (unsigned long long)st.capacity;
@@ -1235,12 +1268,13 @@ MPM_DI void store_reserve(const MpmGridStore& st, int slot, int n) {
 }
 
 // List of flagged blocks (warp-aggregated append; order is not significant).
+// Every flag read is cleared, so the flags are clean for the next substep.
 // The appending warp zeroes its blocks in grids a and b (either may be null).
 // With reserve_slot >= 0 the last CTA to finish (threadfence + ticket, no
 // waiting) reserves room for the list in the grid store.  The threads also
 // convert the substep's tool poses (pose_table_fill).
 template <typename T>
-__global__ void __launch_bounds__(256) k_compact_clear(const unsigned char* __restrict__ flags, int64_t total,
+__global__ void __launch_bounds__(256) k_compact_clear(unsigned char* __restrict__ flags, int64_t total,
                                                        int* __restrict__ active, int* __restrict__ counter,
                                                        unsigned* __restrict__ ticket, Node<T>* __restrict__ a,
                                                        Node<T>* __restrict__ b, const int64_t* __restrict__ saved,
@@ -1249,6 +1283,7 @@ __global__ void __launch_bounds__(256) k_compact_clear(const unsigned char* __re
   pose_table_fill<T>(pt, i, (int64_t)gridDim.x * blockDim.x);
   if (saved && *saved >= 0) return;  // list and grid a restored; b zeroed by the restore
   const bool f = i < total && flags[i] != 0;
+  if (f) flags[i] = 0;
   unsigned m = __ballot_sync(0xffffffffu, f);
   const int lane = threadIdx.x & 31;
   if (m) {
@@ -1282,44 +1317,6 @@ __global__ void __launch_bounds__(256) k_compact_clear(const unsigned char* __re
       __threadfence();
       store_reserve(store, reserve_slot, atomicAdd(counter, 0));
     }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// grid store: the forward grid of a substep (its active blocks) is kept so
-// the adjoint substep restores it instead of recomputing p2g
-// ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(256) k_store_copy(MpmGridStore st, int slot, const int* __restrict__ active,
-                                                    const Node<T>* __restrict__ grid) {
-  const int64_t start = st.slot_start[slot];
-  if (start < 0) return;
-  const int64_t n = (int64_t)st.slot_count[slot] * 64;
-  Node<T>* dst = reinterpret_cast<Node<T>*>(st.blocks);
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int blk = active[i >> 6];
-    dst[(start << 6) + i] = grid[(int64_t)blk * 64 + (i & 63)];
-    if ((i & 63) == 0) st.block_ids[start + (i >> 6)] = blk;
-  }
-}
-// restore the active list and the grid blocks of a stored substep; the same
-// blocks of grid b (may be null) are zeroed
-template <typename T>
-__global__ void __launch_bounds__(256) k_store_restore(MpmGridStore st, int slot, int* __restrict__ active,
-                                                       int* __restrict__ n_active, Node<T>* __restrict__ grid,
-                                                       Node<T>* __restrict__ b) {
-  const int64_t start = st.slot_start[slot];
-  if (start < 0) return;
-  const int cnt = st.slot_count[slot];
-  if (blockIdx.x == 0 && threadIdx.x == 0) *n_active = cnt;
-  const Node<T>* src = reinterpret_cast<const Node<T>*>(st.blocks);
-  const Node<T> z = {T(0), T(0), T(0), T(0)};
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)cnt * 64;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int blk = st.block_ids[start + (i >> 6)];
-    if ((i & 63) == 0) active[i >> 6] = blk;
-    grid[(int64_t)blk * 64 + (i & 63)] = src[(start << 6) + i];
-    if (b) b[(int64_t)blk * 64 + (i & 63)] = z;
   }
 }
 

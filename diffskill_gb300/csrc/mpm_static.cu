@@ -80,9 +80,11 @@ int scratch_base(int dev, unsigned char** out) {
       return set_err(MPM_E_CUDA, std::string("mpm_substep_fwd_static: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     unsigned char* base = static_cast<unsigned char*>(p);
     e = cudaMemset(base + kHeader, 0, kScene);
+    // block flags start clean; every compaction clears the flags it reads
+    if (e == cudaSuccess) e = cudaMemset(base + kBlockBuf, 0, 16 + kMaxBlocks);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess)
-      return set_err(MPM_E_CUDA, std::string("mpm_substep_fwd_static: clearing the scene index: ") +
+      return set_err(MPM_E_CUDA, std::string("mpm_substep_fwd_static: clearing the scene index and block flags: ") +
                                      cudaGetErrorString(e));
     g_base[dev] = base;
   }
@@ -163,7 +165,7 @@ int mpm_substep_fwd_static(const MpmParams* params, const MpmToolDesc* tools, in
   L.grid_b = base + kHeader + kScene + grid_bytes;  // fully written by grid_op
   L.grid_c = nullptr;
   L.grid_d = nullptr;
-  L.blockbuf = base + kBlockBuf;  // cleared by the launcher every call
+  L.blockbuf = base + kBlockBuf;  // flags cleared once above, then by every compaction
   L.active = reinterpret_cast<int*>(base + kActive);
   L.contact = nullptr;  // forward only
   L.tools_t = base + kToolsT;
