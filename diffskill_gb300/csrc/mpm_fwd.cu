@@ -55,9 +55,11 @@ cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, 
   unsigned* ticket = reinterpret_cast<unsigned*>(L.blockbuf + 4);
   unsigned char* flags = L.blockbuf + 16;
   const int64_t* saved = restore ? restore->slot_start + restore_slot : nullptr;
-  const unsigned cap = (unsigned)(L.sm_count * 16);
+  // one thread per particle for the marking; the restore strides over the stored nodes
   unsigned mb = blocks_for(c.n_particles, 256);
-  mb = restore ? cap : (mb < cap ? (mb > 0 ? mb : 1) : cap);
+  const unsigned floor_ctas = (unsigned)(L.sm_count * 8);
+  if (restore && mb < floor_ctas) mb = floor_ctas;
+  if (mb == 0) mb = 1;
   MpmGridStore rst{};
   if (restore) rst = *restore;
   MPM_LAUNCH(L, MPM_K_CLEAR, k_mark_or_restore<T>, mb, 256, c, st, L.pscene, flags, counter, rst,

@@ -1229,10 +1229,11 @@ __global__ void __launch_bounds__(256) k_mark_or_restore(Consts<T> c, const T* _
     if (p < c.n_particles) {
       T x[3];
       load_row(st, c.ld, p, 0, 3, x);
+      const int sc = pscene[p];  // issued with the x loads
       Stencil<T> s;
       ok = make_stencil(c, x, s);  // out-of-grid particles are skipped (and flagged) by the scatter
       if (ok) {
-        scene = pscene[p];
+        scene = sc;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
           lo[d] = s.base[d] >> 2;
