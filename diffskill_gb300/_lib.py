@@ -12,7 +12,7 @@ from typing import Optional
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmpm_gb300.so")
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 MPM_OK = 0
 STATUS_OUT_OF_GRID = 1
 STATUS_NONFINITE = 2

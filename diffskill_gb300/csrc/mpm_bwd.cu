@@ -8,8 +8,8 @@ namespace mpm {
 template <typename T>
 Consts<T> make_consts(const LaunchCtx& L);  // mpm_fwd.cu
 template <typename T>
-cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* b,
-                           const MpmGridStore* restore, int restore_slot, const MpmGridStore* reserve,
+cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* a_out,
+                           Node<T>* b, const MpmGridStore* restore, int restore_slot, const MpmGridStore* reserve,
                            int reserve_slot, const double* pose_f, const double* pose_f1);
 unsigned grid_blocks_launch(const LaunchCtx& L, int64_t total_blocks);
 
@@ -27,24 +27,26 @@ cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* st1, c
   const int* counter = reinterpret_cast<const int*>(L.blockbuf);
   const unsigned pb = blocks_for(c.n_particles, 128);
   const unsigned gb = grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3);
-  // recompute the grid of this substep (substep_grad, mpm_simulator.py:327-333)
-  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, g_gout, store, slot, nullptr, -1, pose_f, pose_f1);
+  // recompute the grids of this substep (substep_grad, mpm_simulator.py:327-333)
+  // unless the grid store holds them (then p2g and grid_op return at once)
+  const int64_t* saved = store ? store->slot_start + slot : nullptr;
+  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, gout, g_gout, store, slot, nullptr, -1, pose_f, pose_f1);
   if (e != cudaSuccess) return e;
   if (c.n_particles > 0) {
     // with a grid store the recompute usually exits at once: a grid of one
     // wave of CTAs that stride over the particles
     const unsigned cap = (unsigned)(L.sm_count * 6);
     MPM_LAUNCH(L, MPM_K_P2G_RECOMP, (k_p2g<T, S, true>), store && pb > cap ? cap : pb, 128, c, st0, (T*)nullptr,
-               L.pscene, gin, store ? store->slot_start + slot : (const int64_t*)nullptr);
+               L.pscene, gin, saved);
   }
   const Tool<T>* tools_t = (const Tool<T>*)L.tools_t;
   const T* poses_t = (const T*)L.poses_t;
   MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, gb, 64, c, L.active, counter, gin, gout, tools_t, poses_t, L.tool_off,
-             L.contact, MpmGridStore{}, -1);
+             MpmGridStore{}, -1, saved);
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_G2P_ADJ, k_g2p_adj<T>, pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
   MPM_LAUNCH(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, gb, 64, c, L.active, counter, gin, g_gout, g_gin, tools_t,
-             poses_t, L.tool_off, (const unsigned char*)L.contact, g_pose_f, g_pose_f1);
+             poses_t, L.tool_off, g_pose_f, g_pose_f1);
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_P2G_ADJ, (k_p2g_adj<T, S>), pb, 128, c, st0, g1, g0, L.pscene, g_gin);
   return cudaGetLastError();

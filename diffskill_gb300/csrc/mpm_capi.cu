@@ -34,7 +34,6 @@ struct MpmHandle {
   void* grid[4] = {nullptr, nullptr, nullptr, nullptr};
   unsigned char* d_blockbuf = nullptr;
   int* d_active = nullptr;
-  unsigned char* d_contact = nullptr;  // per active-list block: touched by a tool (adjoint)
   void* d_tools_t = nullptr;  // tools in the compute precision (converted by mpm_set_tools)
   void* d_poses_t = nullptr;  // poses of the current substep in the compute precision
   int sm_count = 1;
@@ -106,7 +105,6 @@ mpm::LaunchCtx ctx(MpmHandle* h, void* stream) {
   L.grid_d = h->grid[3];
   L.blockbuf = h->d_blockbuf;
   L.active = h->d_active;
-  L.contact = h->d_contact;
   L.tools_t = h->d_tools_t;
   L.poses_t = h->d_poses_t;
   L.sm_count = h->sm_count;
@@ -139,7 +137,7 @@ int check_aligned(MpmHandle* h, const void* ptr, const char* name, bool allow_nu
 
 extern "C" {
 
-const char* mpm_version(void) { return "mpm_gb300 2 (sm_103a)"; }
+const char* mpm_version(void) { return "mpm_gb300 3 (sm_103a)"; }
 
 int mpm_create(const MpmParams* params, const int64_t* scene_offsets, MpmHandle** out) {
   if (!params || !scene_offsets || !out) return fail(nullptr, MPM_E_INVALID, "mpm_create: NULL argument");
@@ -191,7 +189,6 @@ int mpm_create(const MpmParams* params, const int64_t* scene_offsets, MpmHandle*
   // block flags start clean; every compaction clears the flags it reads
   ok = ok && cudaMemset(h->d_blockbuf, 0, mpm::blockbuf_bytes(p.n_scenes, p.n_grid)) == cudaSuccess;
   ok = ok && cudaMalloc(&h->d_active, nblocks * sizeof(int)) == cudaSuccess;
-  ok = ok && cudaMalloc(&h->d_contact, nblocks) == cudaSuccess;
   if (ok) cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
   if (h->sm_count < 1) h->sm_count = 1;
   if (!ok) {
@@ -225,7 +222,6 @@ int mpm_destroy(MpmHandle* h) {
   for (int i = 0; i < 4; ++i) cudaFree(h->grid[i]);
   cudaFree(h->d_blockbuf);
   cudaFree(h->d_active);
-  cudaFree(h->d_contact);
   cudaFree(h->d_tools_t);
   cudaFree(h->d_poses_t);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);

@@ -42,13 +42,14 @@ static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs
 // length at L.blockbuf[0..3] (a ticket counter at [4..7]); the block flags at
 // L.blockbuf + 16 are clean before and after (cleared by the compaction).
 // ``restore`` (may be null): the adjoint's grid store; when its slot holds
-// this substep the list and grid a are restored from it and b is zeroed.
+// this substep the list, grid a and grid a_out (the grid_op output) are
+// restored from it and b is zeroed.
 // ``reserve`` (may be null): the forward's grid store; room for the list is
 // reserved in slot ``reserve_slot`` by the compaction's last CTA.
 // The compaction also fills L.poses_t for the poses pose_f, pose_f1.
 template <typename T>
-cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* b,
-                           const MpmGridStore* restore, int restore_slot, const MpmGridStore* reserve,
+cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* a_out,
+                           Node<T>* b, const MpmGridStore* restore, int restore_slot, const MpmGridStore* reserve,
                            int reserve_slot, const double* pose_f, const double* pose_f1) {
   const int64_t total = (int64_t)c.n_scenes * c.NB3;
   int* counter = reinterpret_cast<int*>(L.blockbuf);
@@ -63,7 +64,7 @@ cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, 
   MpmGridStore rst{};
   if (restore) rst = *restore;
   MPM_LAUNCH(L, MPM_K_CLEAR, k_mark_or_restore<T>, mb, 256, c, st, L.pscene, flags, counter, rst,
-             restore ? restore_slot : -1, L.active, a, b);
+             restore ? restore_slot : -1, L.active, a, a_out, b);
   MpmGridStore rs{};
   if (reserve) rs = *reserve;
   const PoseTableArgs tt{L.n_tools, pose_f, pose_f1, L.poses_t};
@@ -72,11 +73,11 @@ cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, 
   return cudaGetLastError();
 }
 template cudaError_t prepare_blocks<float>(const LaunchCtx&, const Consts<float>&, const float*, Node<float>*,
-                                           Node<float>*, const MpmGridStore*, int, const MpmGridStore*, int,
-                                           const double*, const double*);
+                                           Node<float>*, Node<float>*, const MpmGridStore*, int,
+                                           const MpmGridStore*, int, const double*, const double*);
 template cudaError_t prepare_blocks<double>(const LaunchCtx&, const Consts<double>&, const double*, Node<double>*,
-                                            Node<double>*, const MpmGridStore*, int, const MpmGridStore*, int,
-                                            const double*, const double*);
+                                            Node<double>*, Node<double>*, const MpmGridStore*, int,
+                                            const MpmGridStore*, int, const double*, const double*);
 
 size_t tools_t_bytes(int64_t n_tools) { return (size_t)(n_tools > 0 ? n_tools : 1) * sizeof(Tool<double>); }
 size_t poses_t_bytes(int64_t n_tools) { return (size_t)(n_tools > 0 ? n_tools : 1) * 16 * sizeof(double); }
@@ -102,14 +103,15 @@ cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const d
   Node<T>* gin = (Node<T>*)L.grid_a;
   Node<T>* gout = (Node<T>*)L.grid_b;
   const int* counter = reinterpret_cast<const int*>(L.blockbuf);
-  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, (Node<T>*)nullptr, nullptr, -1, store, slot, pose_f, pose_f1);
+  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, (Node<T>*)nullptr, (Node<T>*)nullptr, nullptr, -1, store, slot,
+                                    pose_f, pose_f1);
   if (e != cudaSuccess) return e;
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S>), blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gin,
                (const int64_t*)nullptr);
   MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3), 64, c, L.active,
              counter, gin, gout, (const Tool<T>*)L.tools_t, (const T*)L.poses_t, L.tool_off,
-             (unsigned char*)nullptr, store ? *store : MpmGridStore{}, store ? slot : -1);
+             store ? *store : MpmGridStore{}, store ? slot : -1, (const int64_t*)nullptr);
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_G2P, k_g2p<T>, blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gout);
   return cudaGetLastError();

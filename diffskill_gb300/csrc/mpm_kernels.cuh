@@ -598,10 +598,9 @@ struct SceneToolView {
   int n;
   const Tool<T>* tool;
   const Pose<T>* pose;
-  // none: a block no tool touches (the adjoint's light path: no tool terms)
-  MPM_DI SceneToolView(const Tool<T>* tools_t, const T* poses_t, const int* tool_off, int scene, bool none = false) {
+  MPM_DI SceneToolView(const Tool<T>* tools_t, const T* poses_t, const int* tool_off, int scene) {
     const int t0 = tool_off[scene];
-    n = none ? 0 : tool_off[scene + 1] - t0;
+    n = tool_off[scene + 1] - t0;
     tool = tools_t + t0;
     pose = reinterpret_cast<const Pose<T>*>(poses_t + 16 * (int64_t)t0);
   }
@@ -685,18 +684,19 @@ MPM_DI void walls_vjp(const Consts<T>& c, const int* I, const WallTape<T>& tp, T
 
 // Per-CTA tool table, reloaded when the block's scene changes.
 // grid_op over the active blocks: one 64-thread CTA per block, grid-stride.
-// contact (may be null): contact[b] = 1 when a tool's contact response was
-// applied to a node of list block b (read by grid_op.grad).
-// store_slot >= 0: list block b of grid_in is also copied to the grid store
-// at slot_start + b (reserved by the compaction; -1 when the store is full)
+// store_slot >= 0: list block b of grid_in and of grid_out are also copied to
+// the grid store at slot_start + b (reserved by the compaction; -1 when the
+// store is full).  saved (may be null; the adjoint's recompute): when it
+// points at a slot start >= 0 both grids were restored from the store and the
+// kernel returns at once.
 template <typename T>
 __global__ void __launch_bounds__(64) k_grid_op(Consts<T> c, const int* __restrict__ active,
                                                 const int* __restrict__ n_active,
                                                 const Node<T>* __restrict__ grid_in, Node<T>* __restrict__ grid_out,
                                                 const Tool<T>* __restrict__ tools_t, const T* __restrict__ poses_t,
-                                                const int* __restrict__ tool_off,
-                                                unsigned char* __restrict__ contact, MpmGridStore store,
-                                                int store_slot) {
+                                                const int* __restrict__ tool_off, MpmGridStore store,
+                                                int store_slot, const int64_t* __restrict__ saved) {
+  if (saved && *saved >= 0) return;
   const int na = *n_active;
   const int64_t start = store_slot >= 0 ? store.slot_start[store_slot] : -1;
   for (int b = blockIdx.x; b < na; b += gridDim.x) {
@@ -706,17 +706,17 @@ __global__ void __launch_bounds__(64) k_grid_op(Consts<T> c, const int* __restri
     const SceneToolView<T> sh(tools_t, poses_t, tool_off, scene);
     const int64_t idx = gb * 64 + threadIdx.x;
     Node<T> in = grid_in[idx];
-    if (start >= 0) {
-      reinterpret_cast<Node<T>*>(store.blocks)[((start + b) << 6) + threadIdx.x] = in;
+    Node<T>* stored = start >= 0 ? reinterpret_cast<Node<T>*>(store.blocks) + ((start + b) << 7) : nullptr;
+    if (stored) {
+      stored[threadIdx.x] = in;
       if (threadIdx.x == 0) store.block_ids[start + b] = (int)gb;
     }
     Node<T> out = {T(0), T(0), T(0), in.w};
-    bool hit = false;
     if (in.w > T(1e-12)) {
       T inv = T(1) / in.w;
       T v[3] = {inv * in.x + c.gdt[0], inv * in.y + c.gdt[1], inv * in.z + c.gdt[2]};
       const T p[3] = {T(I[0]) * c.dx, T(I[1]) * c.dx, T(I[2]) * c.dx};
-      for (int t = 0; t < sh.n; ++t) hit = tool_collide(sh.tool[t], sh.p0(t), sh.p1(t), p, c.dt, v) || hit;
+      for (int t = 0; t < sh.n; ++t) tool_collide(sh.tool[t], sh.p0(t), sh.p1(t), p, c.dt, v);
       walls(c, I, v, (WallTape<T>*)nullptr);
       if (!(finite(v[0]) && finite(v[1]) && finite(v[2]))) atomicOr(c.status, MPM_STATUS_NONFINITE);
       out.x = v[0];
@@ -724,10 +724,7 @@ __global__ void __launch_bounds__(64) k_grid_op(Consts<T> c, const int* __restri
       out.z = v[2];
     }
     grid_out[idx] = out;
-    if (contact) {  // uniform: the adjoint's recompute records the blocks a tool touches
-      const int any = __syncthreads_or(hit);
-      if (threadIdx.x == 0) contact[b] = (unsigned char)(any != 0);
-    }
+    if (stored) stored[64 + threadIdx.x] = out;
   }
 }
 
@@ -1009,16 +1006,13 @@ __global__ void __launch_bounds__(64) k_grid_op_adj(Consts<T> c, const int* __re
                                                     const Node<T>* __restrict__ g_grid, Node<T>* __restrict__ g_in,
                                                     const Tool<T>* __restrict__ tools_t,
                                                     const T* __restrict__ poses_t, const int* __restrict__ tool_off,
-                                                    const unsigned char* __restrict__ contact,
                                                     double* __restrict__ g_pose_f, double* __restrict__ g_pose_f1) {
   const int na = *n_active;
   for (int b = blockIdx.x; b < na; b += gridDim.x) {
     const int64_t gb = active[b];
     int I[3];
     const int scene = block_node(c, gb, threadIdx.x, I);
-    // a block no tool touched in the recompute takes no tool term: its
-    // adjoint passes through the tools unchanged, with zero pose gradients
-    const SceneToolView<T> sh(tools_t, poses_t, tool_off, scene, contact && !contact[b]);
+    const SceneToolView<T> sh(tools_t, poses_t, tool_off, scene);
     const int64_t idx = gb * 64 + threadIdx.x;
     Node<T> in = grid_in[idx];
     Node<T> go = g_grid[idx];
@@ -1187,8 +1181,8 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 4 : 
 // ---------------------------------------------------------------------------
 // Start of a substep's block bookkeeping, one launch:
 // - restore (when the grid store's slot holds this substep): the active list,
-//   its length and grid a come back from the store, and the same blocks of
-//   grid b (may be null) are zeroed;
+//   its length, grid a (p2g) and grid a_out (grid_op output) come back from
+//   the store, and the same blocks of grid b (may be null) are zeroed;
 // - otherwise: the list length and the reservation ticket are reset, and
 //   flags[scene*NB3 + block] = 1 for every block a particle stencil touches.
 //   The flags are clean on entry (the compaction clears every flag it reads).
@@ -1201,7 +1195,8 @@ __global__ void __launch_bounds__(256) k_mark_or_restore(Consts<T> c, const T* _
                                                          const int* __restrict__ pscene,
                                                          unsigned char* __restrict__ flags, int* __restrict__ header,
                                                          MpmGridStore store, int slot, int* __restrict__ active,
-                                                         Node<T>* __restrict__ a, Node<T>* __restrict__ b) {
+                                                         Node<T>* __restrict__ a, Node<T>* __restrict__ a_out,
+                                                         Node<T>* __restrict__ b) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t start = slot >= 0 ? store.slot_start[slot] : -1;
   if (start >= 0) {
@@ -1212,7 +1207,9 @@ __global__ void __launch_bounds__(256) k_mark_or_restore(Consts<T> c, const T* _
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)cnt * 64; i += stride) {
       const int blk = store.block_ids[start + (i >> 6)];
       if ((i & 63) == 0) active[i >> 6] = blk;
-      a[(int64_t)blk * 64 + (i & 63)] = src[(start << 6) + i];
+      const Node<T>* sb = src + ((start + (i >> 6)) << 7) + (i & 63);
+      a[(int64_t)blk * 64 + (i & 63)] = sb[0];
+      if (a_out) a_out[(int64_t)blk * 64 + (i & 63)] = sb[64];
       if (b) b[(int64_t)blk * 64 + (i & 63)] = z;
     }
     return;
@@ -1256,9 +1253,10 @@ __global__ void __launch_bounds__(256) k_mark_or_restore(Consts<T> c, const T* _
   }
 }
 
-// Grid store: the forward grid of a substep (its active blocks) is kept so the
-// adjoint substep restores it instead of recomputing p2g (copy in k_grid_op,
-// restore in k_mark_or_restore).  One thread reserves room for n active blocks
+// Grid store: the forward grids of a substep (the active blocks of the p2g
+// grid and of the grid_op output) are kept so the adjoint substep restores
+// them instead of recomputing p2g and grid_op (copy in k_grid_op, restore in
+// k_mark_or_restore).  One thread reserves room for n active blocks
 // of substep `slot` (bump allocator); slot_start = -1 when the store is full
 // (the adjoint then recomputes)
 MPM_DI void store_reserve(const MpmGridStore& st, int slot, int n) {

@@ -43,7 +43,6 @@ struct LaunchCtx {
   void* grid_d;
   unsigned char* blockbuf;     // [16-byte counter header][n_scenes * NB3 block flags]
   int* active;                 // [n_scenes * NB3] list of active blocks
-  unsigned char* contact;      // [n_scenes * NB3] per list block: a tool touched it (adjoint only; may be null)
   const void* tools_t;         // [n_tools] Tool<T>, converted when the tools are set (convert_tools)
   void* poses_t;               // [n_tools * 16] T: poses of frames f, f+1, converted every substep
   int sm_count;                // multiprocessors of the device (grid-stride launch sizes)

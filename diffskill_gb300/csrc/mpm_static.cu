@@ -167,7 +167,6 @@ int mpm_substep_fwd_static(const MpmParams* params, const MpmToolDesc* tools, in
   L.grid_d = nullptr;
   L.blockbuf = base + kBlockBuf;  // flags cleared once above, then by every compaction
   L.active = reinterpret_cast<int*>(base + kActive);
-  L.contact = nullptr;  // forward only
   L.tools_t = base + kToolsT;
   L.poses_t = base + kPosesT;
   int sm = 1;

@@ -341,14 +341,16 @@ class MpmEngine:
 class GridStore:
     """Caller-owned arena of forward-grid blocks (``MpmGridStore`` of the C ABI).
 
-    Substeps whose forward grid is stored skip the p2g recompute in their
-    adjoint; a substep that does not fit is recomputed (same result).
+    Substeps whose forward grids are stored skip the p2g and grid_op
+    recomputes in their adjoint; a substep that does not fit is recomputed
+    (same result).
     """
 
     def __init__(self, eng: MpmEngine, n_slots: int, capacity_blocks: int):
         dev = eng.device
         self.capacity = int(max(capacity_blocks, 0))
-        self.blocks = torch.empty((max(self.capacity, 1), 64, 4), dtype=eng.dtype, device=dev)
+        # per stored block: the p2g grid block, then the grid_op output block
+        self.blocks = torch.empty((max(self.capacity, 1), 2, 64, 4), dtype=eng.dtype, device=dev)
         self.block_ids = torch.empty(max(self.capacity, 1), dtype=torch.int32, device=dev)
         self.slot_start = torch.full((n_slots,), -1, dtype=torch.int64, device=dev)
         self.slot_count = torch.zeros(n_slots, dtype=torch.int32, device=dev)
@@ -422,7 +424,7 @@ class Horizon:
         self.store = None
         if store_grids:
             n_slots = self.F if k == 1 else k
-            block_bytes = 64 * 4 * (8 if dt == torch.float64 else 4) + 4
+            block_bytes = 2 * 64 * 4 * (8 if dt == torch.float64 else 4) + 4
             if store_budget_bytes is None:
                 free, _ = torch.cuda.mem_get_info(dev)
                 store_budget_bytes = free // 4

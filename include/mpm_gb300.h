@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define MPM_ABI_VERSION 2
+#define MPM_ABI_VERSION 3
 
 /* return codes */
 #define MPM_OK 0
@@ -103,14 +103,15 @@ typedef struct MpmToolDesc {
   double torus[2];      /* Torus tx, ty */
 } MpmToolDesc;
 
-/* Grid store (caller-owned device buffers): the forward grid of a substep,
- * i.e. its active 4x4x4-node blocks, kept so the adjoint substep restores it
- * instead of recomputing p2g.  Slots are filled by a device-side bump
+/* Grid store (caller-owned device buffers): the forward grids of a substep,
+ * i.e. its active 4x4x4-node blocks of the p2g grid and of the grid_op
+ * output, kept so the adjoint substep restores both instead of recomputing
+ * p2g and grid_op.  Slots are filled by a device-side bump
  * allocator; a substep that does not fit gets slot_start = -1 and its adjoint
  * recomputes the grid, so results never depend on the capacity.  Zero *bump
  * (and set slot_start to -1) before reusing slots. */
 typedef struct MpmGridStore {
-  void* blocks;                 /* real[capacity][64][4] */
+  void* blocks;                 /* real[capacity][2][64][4]: p2g grid block, grid_op output block */
   int32_t* block_ids;           /* [capacity] global block id of each stored block */
   int64_t* slot_start;          /* [n_slots] first stored block of the slot, -1 = not stored */
   int32_t* slot_count;          /* [n_slots] */
