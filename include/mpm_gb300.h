@@ -187,13 +187,14 @@ int mpm_substep_bwd(MpmHandle* h, const void* state_f, const void* state_f1, con
                     void* g_state_f, const double* pose_f, const double* pose_f1, double* g_pose_f,
                     double* g_pose_f1, void* stream);
 
-/* mpm_substep_fwd that also keeps the substep's forward grid in store slot
+/* mpm_substep_fwd that also keeps the substep's forward grids in store slot
  * `slot` (no counterpart in the reference, whose substep_grad always
  * recomputes the grid, mpm_simulator.py:327-333). */
 int mpm_substep_fwd_store(MpmHandle* h, const void* state_f, void* state_f1, const double* pose_f,
                           const double* pose_f1, const MpmGridStore* store, int32_t slot, void* stream);
-/* mpm_substep_bwd that restores the forward grid from store slot `slot` when
- * it was stored, and recomputes it otherwise. */
+/* mpm_substep_bwd that restores the forward grids (p2g grid and grid_op
+ * output) from store slot `slot` when they were stored, and recomputes them
+ * otherwise. */
 int mpm_substep_bwd_store(MpmHandle* h, const void* state_f, const void* state_f1, const void* g_state_f1,
                           void* g_state_f, const double* pose_f, const double* pose_f1, double* g_pose_f,
                           double* g_pose_f1, const MpmGridStore* store, int32_t slot, void* stream);
