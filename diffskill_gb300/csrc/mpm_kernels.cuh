@@ -1244,11 +1244,16 @@ __global__ void __launch_bounds__(256) k_mark_or_restore(Consts<T> c, const T* _
     }
     const unsigned long long prev = __shfl_up_sync(0xffffffffu, key, 1);
     if (ok && (lane == 0 || prev != key)) {
+      // the 1, 2, 4 or 8 blocks (lo + {0, ext}) as predicated stores; the
+      // offset within a scene fits 32 bits (nb <= 256)
       unsigned char* f = flags + (int64_t)scene * c.NB3;
       const int nb = c.nb;
-      for (int bi = lo[0]; bi <= lo[0] + ext[0]; ++bi)
-        for (int bj = lo[1]; bj <= lo[1] + ext[1]; ++bj)
-          for (int bk = lo[2]; bk <= lo[2] + ext[2]; ++bk) f[((int64_t)bi * nb + bj) * nb + bk] = 1;
+      const int i0 = (lo[0] * nb + lo[1]) * nb + lo[2];
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const int di = m >> 2, dj = (m >> 1) & 1, dk = m & 1;
+        if (di <= ext[0] && dj <= ext[1] && dk <= ext[2]) f[i0 + (di * nb + dj) * nb + dk] = 1;
+      }
     }
   }
 }
