@@ -743,9 +743,11 @@ __global__ void __launch_bounds__(128) k_g2p(Consts<T> c, const T* __restrict__ 
   }
   const Node<T>* g = grid + (int64_t)pscene[p] * c.G;
   const StencilAddr A = stencil_addr(c, s);
-  T nv[3] = {T(0), T(0), T(0)}, nC[9];
+  // C = k4 sum_o wgt v(o) (o - fx)^T = k4 (m1 - nv fx^T) with m1 = sum_o wgt v(o) o^T:
+  // the offsets o are 0, 1, 2, so m1 takes only additions
+  T nv[3] = {T(0), T(0), T(0)}, m1[9], nC[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) nC[k] = T(0);
+  for (int k = 0; k < 9; ++k) m1[k] = T(0);
   const T k4 = T(4) * c.inv_dx;
 #pragma unroll
   for (int ox = 0; ox < 3; ++ox)
@@ -755,15 +757,22 @@ __global__ void __launch_bounds__(128) k_g2p(Consts<T> c, const T* __restrict__ 
       for (int oz = 0; oz < 3; ++oz) {
         T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
         Node<T> gv = g[A.at(ox, oy, oz)];
-        const T gvv[3] = {gv.x, gv.y, gv.z};
-        const T dp[3] = {T(ox) - s.fx[0], T(oy) - s.fx[1], T(oz) - s.fx[2]};
+        const T q[3] = {wgt * gv.x, wgt * gv.y, wgt * gv.z};
+        const int o[3] = {ox, oy, oz};
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          nv[i] += wgt * gvv[i];
+          nv[i] += q[i];
 #pragma unroll
-          for (int j = 0; j < 3; ++j) nC[i * 3 + j] += k4 * wgt * gvv[i] * dp[j];
+          for (int j = 0; j < 3; ++j) {
+            if (o[j] == 1) m1[i * 3 + j] += q[i];
+            if (o[j] == 2) m1[i * 3 + j] += T(2) * q[i];
+          }
         }
       }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) nC[i * 3 + j] = k4 * (m1[i * 3 + j] - s.fx[j] * nv[i]);
   T xn[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
