@@ -1070,9 +1070,10 @@ __global__ void __launch_bounds__(64) k_grid_op_adj(Consts<T> c, const int* __re
 
 // p2g.grad + svd_grad + compute_F_tmp.grad: gathers g_in; reads the partial
 // x gradient left in g0 by k_g2p_adj and writes all 24 rows of g0.
-// FP32: at most 128 registers (4 CTAs of 128 threads per SM)
+// FP32: at most 102 registers (5 CTAs of 128 threads per SM; a small spill),
+// measured 3 % faster than 4 CTAs at 128 registers
 template <typename T, typename S>
-__global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 4 : 2) k_p2g_adj(Consts<T> c, const T* __restrict__ st, const T* __restrict__ g1,
+__global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 5 : 2) k_p2g_adj(Consts<T> c, const T* __restrict__ st, const T* __restrict__ g1,
                                                  T* __restrict__ g0, const int* __restrict__ pscene,
                                                  const Node<T>* __restrict__ g_in) {
   int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1118,8 +1119,9 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 4 : 
 #pragma unroll
       for (int b = 0; b < 3; ++b) gw[a][b] = T(0);
     // q(o) = wgt(o) gn(o) and sq = sum_o q(o): the adjoints of m v (gv = m sq) and of
-    // dp = (o - fx) dx through A dp (gfx = -dx A^T sq) need only the sum; the node
-    // value m v + A dp is stepped across the stencil by the columns of dx A
+    // dp = (o - fx) dx through A dp (gfx = -dx A^T sq) need only the sum; the adjoint
+    // of A (ga = sum_o q dp^T) takes sum_o q o^T, additions only as o is 0, 1, 2; the
+    // node value m v + A dp is stepped across the stencil by the columns of dx A
     T sq[3] = {T(0), T(0), T(0)};
     T ad[9], cx[3];
 #pragma unroll
@@ -1135,7 +1137,7 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 4 : 
 #pragma unroll
         for (int oz = 0; oz < 3; ++oz) {
           T wgt = s.w[ox][0] * s.w[oy][1] * s.w[oz][2];
-          const T dp[3] = {(T(ox) - s.fx[0]) * c.dx, (T(oy) - s.fx[1]) * c.dx, (T(oz) - s.fx[2]) * c.dx};
+          const int o[3] = {ox, oy, oz};
           Node<T> n = gg[A.at(ox, oy, oz)];
           const T gn[3] = {n.x, n.y, n.z};
           T g_wgt = dot3(gn, cz) + n.w * c.p_mass;
@@ -1144,7 +1146,10 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 4 : 
             const T q = wgt * gn[k];
             sq[k] += q;
 #pragma unroll
-            for (int j = 0; j < 3; ++j) ga[3 * k + j] += q * dp[j];
+            for (int j = 0; j < 3; ++j) {
+              if (o[j] == 1) ga[3 * k + j] += q;
+              if (o[j] == 2) ga[3 * k + j] += T(2) * q;
+            }
           }
           gw[ox][0] += g_wgt * s.w[oy][1] * s.w[oz][2];
           gw[oy][1] += g_wgt * s.w[ox][0] * s.w[oz][2];
@@ -1158,6 +1163,11 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 4 : 
 #pragma unroll
       for (int k = 0; k < 3; ++k) cx[k] += ad[3 * k];
     }
+    // ga = sum_o q (o - fx)^T dx from its accumulated sum_o q o^T
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) ga[3 * k + j] = c.dx * (ga[3 * k + j] - s.fx[j] * sq[k]);
     T gfx[3];
 #pragma unroll
     for (int j = 0; j < 3; ++j) gfx[j] = -(ad[j] * sq[0] + ad[3 + j] * sq[1] + ad[6 + j] * sq[2]);
