@@ -548,12 +548,12 @@ MPM_DI void p2g_chunk(const Consts<T>& c, const T* __restrict__ st, T* __restric
     }
   }
 }
-// FP32: 6 CTAs of 128 threads per SM (at most 85 registers, no spill);
-// measured 8 % faster than the unconstrained 93 registers
+// FP32: 7 CTAs of 128 threads per SM (at most 73 registers, no spill);
+// measured 6 % faster than 6 CTAs
 // Strided: the CTAs stride over the particle chunks (the adjoint's recompute,
 // which exits at once when the grid store holds the substep)
 template <typename T, typename S, bool Strided = false>
-__global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 6 : 4) k_p2g(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
+__global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 7 : 4) k_p2g(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
                                              const int* __restrict__ pscene, Node<T>* __restrict__ grid,
                                              const int64_t* __restrict__ saved) {
   if (saved && *saved >= 0) return;  // the grid of this substep was restored from the grid store
