@@ -438,17 +438,35 @@ MPM_DI void local_sdf_grad(const Tool<T>& t, const T* q, T gap, T g, T* gq, T* g
   }
   box_sdf_grad(t.size, q, g, gq);
 }
-// finite-difference normal before normalisation (Box._normal, Knife._normal)
+// finite-difference normal before normalisation (Box._normal, Knife._normal);
+// only box-type shapes (Box, Gripper fingers) and the Knife come here.  The
+// shape test is taken once, so the six SDF evaluations are straight-line code
+// that the compiler can interleave.
+template <typename T>
+MPM_DI T knife_sdf(const Tool<T>& t, const T* q) {
+  T a = prism_sdf(t, q), b = box_sdf(t.size, q);
+  return (b < a) ? a : b;
+}
 template <typename T>
 MPM_DI void fd_normal_raw(const Tool<T>& t, const T* q, T* r) {
   const T d = fd_step<T>();
   const T h = T(0.5) / d;
+  if (t.type == TOOL_KNIFE) {
 #pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    T inc[3] = {q[0], q[1], q[2]}, dec[3] = {q[0], q[1], q[2]};
-    inc[i] += d;
-    dec[i] -= d;
-    r[i] = h * (local_sdf(t, inc, T(0)) - local_sdf(t, dec, T(0)));
+    for (int i = 0; i < 3; ++i) {
+      T inc[3] = {q[0], q[1], q[2]}, dec[3] = {q[0], q[1], q[2]};
+      inc[i] += d;
+      dec[i] -= d;
+      r[i] = h * (knife_sdf(t, inc) - knife_sdf(t, dec));
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      T inc[3] = {q[0], q[1], q[2]}, dec[3] = {q[0], q[1], q[2]};
+      inc[i] += d;
+      dec[i] -= d;
+      r[i] = h * (box_sdf(t.size, inc) - box_sdf(t.size, dec));
+    }
   }
 }
 template <typename T>
@@ -488,13 +506,24 @@ MPM_DI void local_normal_vjp(const Tool<T>& t, const T* q, T gap, const T* gn, T
   unit14_vjp(r, gn, gr);
   const T d = fd_step<T>();
   const T h = T(0.5) / d;
+  if (t.type == TOOL_KNIFE) {
 #pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    T inc[3] = {q[0], q[1], q[2]}, dec[3] = {q[0], q[1], q[2]};
-    inc[i] += d;
-    dec[i] -= d;
-    local_sdf_grad(t, inc, T(0), h * gr[i], gq, (T*)nullptr);
-    local_sdf_grad(t, dec, T(0), -h * gr[i], gq, (T*)nullptr);
+    for (int i = 0; i < 3; ++i) {
+      T inc[3] = {q[0], q[1], q[2]}, dec[3] = {q[0], q[1], q[2]};
+      inc[i] += d;
+      dec[i] -= d;
+      local_sdf_grad(t, inc, T(0), h * gr[i], gq, (T*)nullptr);
+      local_sdf_grad(t, dec, T(0), -h * gr[i], gq, (T*)nullptr);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      T inc[3] = {q[0], q[1], q[2]}, dec[3] = {q[0], q[1], q[2]};
+      inc[i] += d;
+      dec[i] -= d;
+      box_sdf_grad(t.size, inc, h * gr[i], gq);
+      box_sdf_grad(t.size, dec, -h * gr[i], gq);
+    }
   }
 }
 
