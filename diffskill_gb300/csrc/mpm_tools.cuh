@@ -469,8 +469,9 @@ MPM_DI void fd_normal_raw(const Tool<T>& t, const T* q, T* r) {
     }
   }
 }
+// r_out (may be null): the vector before normalisation, for local_normal_vjp
 template <typename T>
-MPM_DI void local_normal(const Tool<T>& t, const T* q, T gap, T* n) {
+MPM_DI void local_normal(const Tool<T>& t, const T* q, T gap, T* n, T* r_out = nullptr) {
   if (dual_shape(t.type)) {
     dual_normal(t, q, gap, n);
     return;
@@ -485,9 +486,16 @@ MPM_DI void local_normal(const Tool<T>& t, const T* q, T gap, T* n) {
   T iL = T(1) / len14(r);
 #pragma unroll
   for (int k = 0; k < 3; ++k) n[k] = r[k] * iL;
+  if (r_out) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r_out[k] = r[k];
+  }
 }
+// r_in (may be null): the r_out of local_normal at the same q (saves the six
+// SDF evaluations of a finite-difference normal)
 template <typename T>
-MPM_DI void local_normal_vjp(const Tool<T>& t, const T* q, T gap, const T* gn, T* gq, T* ggap) {
+MPM_DI void local_normal_vjp(const Tool<T>& t, const T* q, T gap, const T* gn, T* gq, T* ggap,
+                             const T* r_in = nullptr) {
   if (dual_shape(t.type)) {
     dual_normal_vjp(t, q, gap, gn, gq, ggap);
     return;
@@ -502,7 +510,12 @@ MPM_DI void local_normal_vjp(const Tool<T>& t, const T* q, T gap, const T* gn, T
     gq[2] += gr[2];
     return;
   }
-  fd_normal_raw(t, q, r);
+  if (r_in) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[k] = r_in[k];
+  } else {
+    fd_normal_raw(t, q, r);
+  }
   unit14_vjp(r, gn, gr);
   const T d = fd_step<T>();
   const T h = T(0.5) / d;
@@ -557,8 +570,10 @@ MPM_DI void shape_sdf_vjp(const Tool<T>& t, const T* pos, const T* rot, T gap, c
   local_sdf_grad(t, q, gap, g, gq, ggap);
   inv_trans_vjp(p, pos, rot, gq, gp, gpos, grot);
 }
+// r_out (may be null): the local normal before normalisation, for shape_normal_vjp
 template <typename T>
-MPM_DI void shape_normal(const Tool<T>& t, const T* pos, const T* rot, T gap, const T* p, T* n) {
+MPM_DI void shape_normal(const Tool<T>& t, const T* pos, const T* rot, T gap, const T* p, T* n,
+                         T* r_out = nullptr) {
   if (t.type == TOOL_SPHERE) {
     const T d[3] = {p[0] - pos[0], p[1] - pos[1], p[2] - pos[2]};
     T iL = T(1) / len14(d);
@@ -568,13 +583,14 @@ MPM_DI void shape_normal(const Tool<T>& t, const T* pos, const T* rot, T gap, co
   }
   T q[3], nl[3];
   inv_trans(p, pos, rot, q);
-  local_normal(t, q, gap, nl);
+  local_normal(t, q, gap, nl, r_out);
   qrot(rot, nl, n);
 }
-// gp (the point's gradient) and ggap may be NULL
+// gp (the point's gradient) and ggap may be NULL; r_in (may be null): the
+// r_out of shape_normal at the same pose and point
 template <typename T>
 MPM_DI void shape_normal_vjp(const Tool<T>& t, const T* pos, const T* rot, T gap, const T* p, const T* gn, T* gp,
-                             T* gpos, T* grot, T* ggap) {
+                             T* gpos, T* grot, T* ggap, const T* r_in = nullptr) {
   if (t.type == TOOL_SPHERE) {
     const T d[3] = {p[0] - pos[0], p[1] - pos[1], p[2] - pos[2]};
     T gd[3];
@@ -586,12 +602,20 @@ MPM_DI void shape_normal_vjp(const Tool<T>& t, const T* pos, const T* rot, T gap
     }
     return;
   }
-  T q[3], nl[3];
+  T q[3], nl[3], r[3];
   inv_trans(p, pos, rot, q);
-  local_normal(t, q, gap, nl);
+  if (r_in && !dual_shape(t.type)) {  // the normal from r exactly as local_normal forms it
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[k] = r_in[k];
+    T iL = T(1) / len14(r);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) nl[k] = r[k] * iL;
+  } else {
+    local_normal(t, q, gap, nl, r);
+  }
   T gnl[3] = {T(0), T(0), T(0)}, gq[3] = {T(0), T(0), T(0)};
   qrot_vjp(rot, nl, gn, grot, gnl);
-  local_normal_vjp(t, q, gap, gnl, gq, ggap);
+  local_normal_vjp(t, q, gap, gnl, gq, ggap, r);
   inv_trans_vjp(p, pos, rot, gq, gp, gpos, grot);
 }
 // collider_v (primive_base.py:87-94)
@@ -662,8 +686,8 @@ MPM_DI void collide_vjp(const Tool<T>& t, const T* pos0, const T* rot0, T gap0, 
     for (int k = 0; k < 3; ++k) gvin[k] = gout[k];
     return;
   }
-  T D[3], cv[3], iv[3], vt[3];
-  shape_normal(t, pos0, rot0, gap0, p, D);
+  T D[3], Dr[3], cv[3], iv[3], vt[3];
+  shape_normal(t, pos0, rot0, gap0, p, D, Dr);  // Dr reused by the normal's adjoint
   collider_v(pos0, rot0, pos1, rot1, p, dt, cv);
 #pragma unroll
   for (int k = 0; k < 3; ++k) iv[k] = vin[k] - cv[k];
@@ -716,7 +740,7 @@ MPM_DI void collide_vjp(const Tool<T>& t, const T* pos0, const T* rot0, T gap0, 
   }
   T g_dist = (e < T(1)) ? g_infl * e * (-t.softness) : T(0);
   shape_sdf_vjp(t, pos0, rot0, gap0, p, g_dist, (T*)nullptr, gpos0, grot0, ggap0);
-  shape_normal_vjp(t, pos0, rot0, gap0, p, g_D, (T*)nullptr, gpos0, grot0, ggap0);
+  shape_normal_vjp(t, pos0, rot0, gap0, p, g_D, (T*)nullptr, gpos0, grot0, ggap0, Dr);
   collider_v_vjp(pos0, rot0, pos1, rot1, p, dt, g_cv, gpos0, grot0, gpos1, grot1);
 }
 
