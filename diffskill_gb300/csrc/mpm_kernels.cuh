@@ -805,29 +805,38 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 2) k_g2p_adj(Consts<
   bool ok = false;
   int scene = 0;
   T x[3] = {T(0), T(0), T(0)};
+  T nv[3] = {T(0), T(0), T(0)};
+  T gnv[3] = {T(0), T(0), T(0)}, gC[9], gx[3] = {T(0), T(0), T(0)}, gx1[3] = {T(0), T(0), T(0)};
+#pragma unroll
+  for (int k = 0; k < 9; ++k) gC[k] = T(0);
   if (valid) {
+    // every row this particle needs is requested together with x
     load_row(st, c.ld, p, 0, 3, x);
+    if (st1) load_row(st1, c.ld, p, 3, 3, nv);
+    load_row(g1, c.ld, p, 0, 3, gx1);
+    load_row(g1, c.ld, p, 3, 3, gnv);
+    load_row(g1, c.ld, p, 6, 9, gC);
+    scene = pscene[p];
     ok = make_stencil(c, x, s);
-    if (ok) {
-      scene = pscene[p];
-    } else {
+    if (!ok) {
       zero_stencil(s);
+      scene = 0;
       const T z[3] = {T(0), T(0), T(0)};
       store_row(g0, c.ld, p, 0, 3, z);
     }
+  }
+  if (!ok) {  // no contribution (and no 0 * inf) from particles outside the grid
+#pragma unroll
+    for (int k = 0; k < 3; ++k) nv[k] = gnv[k] = gx1[k] = T(0);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) gC[k] = T(0);
   }
   const int64_t off = (int64_t)scene * c.G;
   const Node<T>* g = grid + off;
   Node<T>* gg = g_grid + off;
   const StencilAddr A = stencil_addr(c, s);
-  T nv[3] = {T(0), T(0), T(0)};
-  T gnv[3] = {T(0), T(0), T(0)}, gC[9], gx[3] = {T(0), T(0), T(0)};
-#pragma unroll
-  for (int k = 0; k < 9; ++k) gC[k] = T(0);
   if (ok) {
-    if (st1) {
-      load_row(st1, c.ld, p, 3, 3, nv);
-    } else {
+    if (!st1) {
 #pragma unroll
       for (int ox = 0; ox < 3; ++ox)
 #pragma unroll
@@ -841,10 +850,6 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 2) k_g2p_adj(Consts<
             nv[2] += wgt * n.z;
           }
     }
-    T gx1[3];
-    load_row(g1, c.ld, p, 0, 3, gx1);
-    load_row(g1, c.ld, p, 3, 3, gnv);
-    load_row(g1, c.ld, p, 6, 9, gC);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       T t = x[i] + c.dt * nv[i];
