@@ -465,6 +465,7 @@ MPM_DI void p2g_chunk(const Consts<T>& c, const T* __restrict__ st, T* __restric
       C[k] = S(st[(int64_t)(6 + k) * c.ld + p]);
       F[k] = S(st[(int64_t)(15 + k) * c.ld + p]);
     }
+    const int sc = pscene[p];  // issued with the state rows
     ok = make_stencil(c, x, s);
     MatConsts<S> m = mat_consts<T, S>(c);
     P2G<S> P;
@@ -477,7 +478,7 @@ MPM_DI void p2g_chunk(const Consts<T>& c, const T* __restrict__ st, T* __restric
     if (!ok) atomicOr(c.status, MPM_STATUS_OUT_OF_GRID);
     if (!finite(P.J)) atomicOr(c.status, MPM_STATUS_NONFINITE);
     if (ok) {
-      scene = pscene[p];
+      scene = sc;
 #pragma unroll
       for (int k = 0; k < 9; ++k) affine[k] = T(aff[k]) * c.dx;
 #pragma unroll
@@ -735,13 +736,14 @@ __global__ void __launch_bounds__(128) k_g2p(Consts<T> c, const T* __restrict__ 
   if (p >= c.n_particles) return;
   T x[3];
   load_row(st, c.ld, p, 0, 3, x);
+  const int scene = pscene[p];  // issued with x
   Stencil<T> s;
   if (!make_stencil(c, x, s)) {  // flagged by k_p2g; the particle keeps its state
 #pragma unroll
     for (int k = 0; k < 15; ++k) st_out[(int64_t)k * c.ld + p] = st[(int64_t)k * c.ld + p];
     return;
   }
-  const Node<T>* g = grid + (int64_t)pscene[p] * c.G;
+  const Node<T>* g = grid + (int64_t)scene * c.G;
   const StencilAddr A = stencil_addr(c, s);
   // C = k4 sum_o wgt v(o) (o - fx)^T = k4 (m1 - nv fx^T) with m1 = sum_o wgt v(o) o^T:
   // the offsets o are 0, 1, 2, so m1 takes only additions
@@ -1098,6 +1100,7 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 5 : 
     C[k] = S(st[(int64_t)(6 + k) * c.ld + p]);
     F[k] = S(st[(int64_t)(15 + k) * c.ld + p]);
   }
+  const int scene = pscene[p];  // issued with the state rows
   Stencil<T> s;
   bool ok = make_stencil(c, x, s);
   MatConsts<S> m = mat_consts<T, S>(c);
@@ -1113,7 +1116,7 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 5 : 
 #pragma unroll
   for (int k = 0; k < 9; ++k) g_aff[k] = S(0);
   if (ok) {
-    const Node<T>* gg = g_in + (int64_t)pscene[p] * c.G;
+    const Node<T>* gg = g_in + (int64_t)scene * c.G;
     const StencilAddr A = stencil_addr(c, s);
     T ga[9];
 #pragma unroll
