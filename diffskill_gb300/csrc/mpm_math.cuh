@@ -211,11 +211,15 @@ MPM_DI void qmul_raw(const T* q, const T* r, T* o) {
   o[2] = r[0] * q[2] + r[1] * q[3] + r[2] * q[0] - r[3] * q[1];
   o[3] = r[0] * q[3] - r[1] * q[2] + r[2] * q[1] + r[3] * q[0];
 }
+// 1 / sqrt(L2): FP64 through rsqrt (within 1 ulp; FP64 divide and square root
+// are long instruction sequences on GB300's FP64 pipe), FP32 as 1 / sqrtf
+MPM_DI double inv_len(double L2) { return rsqrt(L2); }
+MPM_DI float inv_len(float L2) { return 1.0f / sqrtf(L2); }
 template <typename T>
 MPM_DI void qmul(const T* q, const T* r, T* out) {
   T o[4];
   qmul_raw(q, r, o);
-  T inv = T(1) / msqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2] + o[3] * o[3]);
+  T inv = inv_len(o[0] * o[0] + o[1] * o[1] + o[2] * o[2] + o[3] * o[3]);
 #pragma unroll
   for (int i = 0; i < 4; ++i) out[i] = o[i] * inv;
 }
@@ -223,12 +227,11 @@ template <typename T>
 MPM_DI void qmul_vjp(const T* q, const T* r, const T* g, T* gq, T* gr) {
   T o[4];
   qmul_raw(q, r, o);
-  T L2 = o[0] * o[0] + o[1] * o[1] + o[2] * o[2] + o[3] * o[3];
-  T L = msqrt(L2);
-  T on = (o[0] * g[0] + o[1] * g[1] + o[2] * g[2] + o[3] * g[3]) / L2;
+  T iL = inv_len(o[0] * o[0] + o[1] * o[1] + o[2] * o[2] + o[3] * o[3]);
+  T on = (o[0] * g[0] + o[1] * g[1] + o[2] * g[2] + o[3] * g[3]) * iL * iL;
   T go[4];
 #pragma unroll
-  for (int i = 0; i < 4; ++i) go[i] = (g[i] - o[i] * on) / L;
+  for (int i = 0; i < 4; ++i) go[i] = (g[i] - o[i] * on) * iL;
   gq[0] += go[0] * r[0] + go[1] * r[1] + go[2] * r[2] + go[3] * r[3];
   gq[1] += -go[0] * r[1] + go[1] * r[0] - go[2] * r[3] + go[3] * r[2];
   gq[2] += -go[0] * r[2] + go[1] * r[3] + go[2] * r[0] - go[3] * r[1];
