@@ -69,6 +69,7 @@ SIGNATURES = {
     "mpm_collision_pairs": (_i32, [_c_p]),
     "mpm_tools_action": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _i32, _c_p]),
     "mpm_tools_action_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _i32, _c_p]),
+    "mpm_set_chained": (_i32, [_c_p, _i32]),
     "mpm_substep_fwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_substep_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_substep_fwd_store": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, ctypes.POINTER(MpmGridStore), _i32, _c_p]),

@@ -10,7 +10,7 @@ Consts<T> make_consts(const LaunchCtx& L);  // mpm_fwd.cu
 template <typename T>
 cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* a_out,
                            Node<T>* b, const MpmGridStore* restore, int restore_slot, const MpmGridStore* reserve,
-                           int reserve_slot, const double* pose_f, const double* pose_f1);
+                           int reserve_slot, const double* pose_f, const double* pose_f1, bool premarked);
 unsigned grid_blocks_launch(const LaunchCtx& L, int64_t total_blocks);
 
 static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
@@ -30,7 +30,7 @@ cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* st1, c
   // recompute the grids of this substep (substep_grad, mpm_simulator.py:327-333)
   // unless the grid store holds them (then p2g and grid_op return at once)
   const int64_t* saved = store ? store->slot_start + slot : nullptr;
-  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, gout, g_gout, store, slot, nullptr, -1, pose_f, pose_f1);
+  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, gout, g_gout, store, slot, nullptr, -1, pose_f, pose_f1, false);
   if (e != cudaSuccess) return e;
   if (c.n_particles > 0) {
     // with a grid store the recompute usually exits at once: a grid of one

@@ -23,6 +23,8 @@ struct MpmHandle {
   int n_cols = 0;
   MpmToolDesc* d_tools = nullptr;
   int n_tools = 0;
+  bool chained = false;           // mpm_set_chained
+  const void* premarked = nullptr;  // frame whose block flags the last forward g2p set
   std::vector<MpmToolDesc> h_tools;
   unsigned int* d_status = nullptr;
   int* d_flags = nullptr;  // convergence flags of mpm_target_sdf
@@ -391,21 +393,28 @@ static int substep_fwd_impl(MpmHandle* h, const void* state_f, void* state_f1, c
   MPM_TRY(check_aligned(h, pose_f1, "pose_f1", h->n_tools == 0));
   MPM_TRY(check_store(h, store, slot));
   mpm::LaunchCtx L = ctx(h, stream);
+  // chained substeps: the previous forward substep's g2p flagged the blocks of
+  // this substep's input frame
+  const bool pre = h->chained && h->premarked == state_f;
+  const bool next = h->chained;
+  h->premarked = nullptr;
   cudaError_t e;
   switch (h->p.precision) {
     case MPM_PREC_FP32:
       e = mpm::launch_substep_fwd<float, float>(L, (const float*)state_f, (float*)state_f1, pose_f, pose_f1, store,
-                                                slot);
+                                                slot, pre, next);
       break;
     case MPM_PREC_FP32_SVD64:
       e = mpm::launch_substep_fwd<float, double>(L, (const float*)state_f, (float*)state_f1, pose_f, pose_f1, store,
-                                                 slot);
+                                                 slot, pre, next);
       break;
     default:
       e = mpm::launch_substep_fwd<double, double>(L, (const double*)state_f, (double*)state_f1, pose_f, pose_f1,
-                                                  store, slot);
+                                                  store, slot, pre, next);
   }
-  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_substep_fwd");
+  if (e != cudaSuccess) return cuda_fail(h, e, "mpm_substep_fwd");
+  if (next) h->premarked = state_f1;
+  return MPM_OK;
 }
 
 static int substep_bwd_impl(MpmHandle* h, const void* state_f, const void* state_f1, const void* g_state_f1,
@@ -426,6 +435,7 @@ static int substep_bwd_impl(MpmHandle* h, const void* state_f, const void* state
   MPM_TRY(check_aligned(h, g_pose_f1, "g_pose_f1", nt));
   MPM_TRY(check_store(h, store, slot));
   mpm::LaunchCtx L = ctx(h, stream);
+  h->premarked = nullptr;  // the adjoint's compaction may consume the flags
   cudaError_t e;
   switch (h->p.precision) {
     case MPM_PREC_FP32:
@@ -444,6 +454,13 @@ static int substep_bwd_impl(MpmHandle* h, const void* state_f, const void* state
                                                   g_pose_f, g_pose_f1, store, slot);
   }
   return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_substep_bwd");
+}
+
+int mpm_set_chained(MpmHandle* h, int32_t on) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_set_chained: NULL handle");
+  h->chained = on != 0;
+  h->premarked = nullptr;
+  return MPM_OK;
 }
 
 int mpm_substep_fwd(MpmHandle* h, const void* state_f, void* state_f1, const double* pose_f, const double* pose_f1,

@@ -47,10 +47,12 @@ static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs
 // ``reserve`` (may be null): the forward's grid store; room for the list is
 // reserved in slot ``reserve_slot`` by the compaction's last CTA.
 // The compaction also fills L.poses_t for the poses pose_f, pose_f1.
+// premarked (forward only): the flags and the header were set by the previous
+// substep's g2p, so the marking launch is skipped.
 template <typename T>
 cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, Node<T>* a, Node<T>* a_out,
                            Node<T>* b, const MpmGridStore* restore, int restore_slot, const MpmGridStore* reserve,
-                           int reserve_slot, const double* pose_f, const double* pose_f1) {
+                           int reserve_slot, const double* pose_f, const double* pose_f1, bool premarked) {
   const int64_t total = (int64_t)c.n_scenes * c.NB3;
   int* counter = reinterpret_cast<int*>(L.blockbuf);
   unsigned* ticket = reinterpret_cast<unsigned*>(L.blockbuf + 4);
@@ -63,8 +65,9 @@ cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, 
   if (mb == 0) mb = 1;
   MpmGridStore rst{};
   if (restore) rst = *restore;
-  MPM_LAUNCH(L, MPM_K_CLEAR, k_mark_or_restore<T>, mb, 256, c, st, L.pscene, flags, counter, rst,
-             restore ? restore_slot : -1, L.active, a, a_out, b);
+  if (!premarked || restore)
+    MPM_LAUNCH(L, MPM_K_CLEAR, k_mark_or_restore<T>, mb, 256, c, st, L.pscene, flags, counter, rst,
+               restore ? restore_slot : -1, L.active, a, a_out, b);
   MpmGridStore rs{};
   if (reserve) rs = *reserve;
   const PoseTableArgs tt{L.n_tools, pose_f, pose_f1, L.poses_t};
@@ -74,10 +77,10 @@ cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, 
 }
 template cudaError_t prepare_blocks<float>(const LaunchCtx&, const Consts<float>&, const float*, Node<float>*,
                                            Node<float>*, Node<float>*, const MpmGridStore*, int,
-                                           const MpmGridStore*, int, const double*, const double*);
+                                           const MpmGridStore*, int, const double*, const double*, bool);
 template cudaError_t prepare_blocks<double>(const LaunchCtx&, const Consts<double>&, const double*, Node<double>*,
                                             Node<double>*, Node<double>*, const MpmGridStore*, int,
-                                            const MpmGridStore*, int, const double*, const double*);
+                                            const MpmGridStore*, int, const double*, const double*, bool);
 
 size_t tools_t_bytes(int64_t n_tools) { return (size_t)(n_tools > 0 ? n_tools : 1) * sizeof(Tool<double>); }
 size_t poses_t_bytes(int64_t n_tools) { return (size_t)(n_tools > 0 ? n_tools : 1) * 16 * sizeof(double); }
@@ -98,13 +101,14 @@ unsigned grid_blocks_launch(const LaunchCtx& L, int64_t total_blocks) {
 
 template <typename T, typename S>
 cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const double* pose_f,
-                               const double* pose_f1, const MpmGridStore* store, int slot) {
+                               const double* pose_f1, const MpmGridStore* store, int slot, bool premarked,
+                               bool mark_next) {
   Consts<T> c = make_consts<T>(L);
   Node<T>* gin = (Node<T>*)L.grid_a;
   Node<T>* gout = (Node<T>*)L.grid_b;
   const int* counter = reinterpret_cast<const int*>(L.blockbuf);
   cudaError_t e = prepare_blocks<T>(L, c, st0, gin, (Node<T>*)nullptr, (Node<T>*)nullptr, nullptr, -1, store, slot,
-                                    pose_f, pose_f1);
+                                    pose_f, pose_f1, premarked);
   if (e != cudaSuccess) return e;
   if (c.n_particles > 0)
     MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S>), blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gin,
@@ -113,7 +117,8 @@ cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const d
              counter, gin, gout, (const Tool<T>*)L.tools_t, (const T*)L.poses_t, L.tool_off,
              store ? *store : MpmGridStore{}, store ? slot : -1, (const int64_t*)nullptr);
   if (c.n_particles > 0)
-    MPM_LAUNCH(L, MPM_K_G2P, k_g2p<T>, blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gout);
+    MPM_LAUNCH(L, MPM_K_G2P, k_g2p<T>, blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gout,
+               mark_next ? L.blockbuf + 16 : (unsigned char*)nullptr, reinterpret_cast<int*>(L.blockbuf));
   return cudaGetLastError();
 }
 
@@ -238,7 +243,7 @@ template cudaError_t launch_tool_distance<double>(const LaunchCtx&, const int*, 
 
 #define MPM_INST_FWD(T, S)                                                                             \
   template cudaError_t launch_substep_fwd<T, S>(const LaunchCtx&, const T*, T*, const double*, const double*, \
-                                                const MpmGridStore*, int);
+                                                const MpmGridStore*, int, bool, bool);
 MPM_INST_FWD(float, float)
 MPM_INST_FWD(float, double)
 MPM_INST_FWD(double, double)

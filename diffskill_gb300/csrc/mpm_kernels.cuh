@@ -437,6 +437,43 @@ MPM_DI MatConsts<S> mat_consts(const Consts<T>& c) {
   return m;
 }
 
+// flags[scene*NB3 + block] = 1 for the blocks of the stencil at `base` (a lane
+// with ok), called by all 32 lanes of a warp.  In cell order neighbouring
+// particles touch the same blocks, so a lane whose (scene, block range)
+// equals the previous lane's writes nothing: about one flag store per block
+// per warp instead of one per particle.
+template <typename T>
+MPM_DI void mark_stencil_blocks(const Consts<T>& c, bool ok, const int* base, int scene,
+                                unsigned char* __restrict__ flags) {
+  const int lane = threadIdx.x & 31;
+  int lo[3] = {0, 0, 0}, ext[3] = {0, 0, 0};
+  unsigned long long key = ~0ull;
+  if (ok) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = base[d] >> 2;
+      ext[d] = ((base[d] + 2) >> 2) - lo[d];  // 0 or 1
+    }
+    // n_grid <= 1024: block coordinates fit 9 bits
+    key = ((unsigned long long)scene << 30) | ((unsigned long long)lo[0] << 21) |
+          ((unsigned long long)lo[1] << 12) | ((unsigned long long)lo[2] << 3) |
+          (unsigned long long)(ext[0] << 2 | ext[1] << 1 | ext[2]);
+  }
+  const unsigned long long prev = __shfl_up_sync(0xffffffffu, key, 1);
+  if (ok && (lane == 0 || prev != key)) {
+    // the 1, 2, 4 or 8 blocks (lo + {0, ext}) as predicated stores; the
+    // offset within a scene fits 32 bits (nb <= 256)
+    unsigned char* f = flags + (int64_t)scene * c.NB3;
+    const int nb = c.nb;
+    const int i0 = (lo[0] * nb + lo[1]) * nb + lo[2];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const int di = m >> 2, dj = (m >> 1) & 1, dk = m & 1;
+      if (di <= ext[0] && dj <= ext[1] && dk <= ext[2]) f[i0 + (di * nb + dj) * nb + dk] = 1;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // forward kernels
 // ---------------------------------------------------------------------------
@@ -729,19 +766,19 @@ __global__ void __launch_bounds__(64) k_grid_op(Consts<T> c, const int* __restri
   }
 }
 
+// g2p of particle p (mpm_simulator.py:265-284): writes rows 0..14 of st_out
+// and xn; returns false (the state copied unchanged) for a particle whose
+// stencil left the grid
 template <typename T>
-__global__ void __launch_bounds__(128) k_g2p(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
-                                             const int* __restrict__ pscene, const Node<T>* __restrict__ grid) {
-  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= c.n_particles) return;
+MPM_DI bool g2p_particle(const Consts<T>& c, const T* __restrict__ st, T* __restrict__ st_out, int64_t p, int scene,
+                         const Node<T>* __restrict__ grid, T* xn) {
   T x[3];
   load_row(st, c.ld, p, 0, 3, x);
-  const int scene = pscene[p];  // issued with x
   Stencil<T> s;
   if (!make_stencil(c, x, s)) {  // flagged by k_p2g; the particle keeps its state
 #pragma unroll
     for (int k = 0; k < 15; ++k) st_out[(int64_t)k * c.ld + p] = st[(int64_t)k * c.ld + p];
-    return;
+    return false;
   }
   const Node<T>* g = grid + (int64_t)scene * c.G;
   const StencilAddr A = stencil_addr(c, s);
@@ -775,7 +812,6 @@ __global__ void __launch_bounds__(128) k_g2p(Consts<T> c, const T* __restrict__ 
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) nC[i * 3 + j] = k4 * (m1[i * 3 + j] - s.fx[j] * nv[i]);
-  T xn[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     T t = x[i] + c.dt * nv[i];
@@ -785,6 +821,31 @@ __global__ void __launch_bounds__(128) k_g2p(Consts<T> c, const T* __restrict__ 
   store_row(st_out, c.ld, p, 0, 3, xn);
   store_row(st_out, c.ld, p, 3, 3, nv);
   store_row(st_out, c.ld, p, 6, 9, nC);
+  return true;
+}
+// mark (may be null; chained forward substeps): also flags the blocks the
+// stencils of the new positions touch, for the next substep, whose
+// compaction reads them instead of a marking pass; header[0..1] (list length,
+// reservation ticket) are reset for that substep.
+template <typename T>
+__global__ void __launch_bounds__(128) k_g2p(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
+                                             const int* __restrict__ pscene, const Node<T>* __restrict__ grid,
+                                             unsigned char* __restrict__ mark, int* __restrict__ header) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = p < c.n_particles;
+  const int scene = valid ? pscene[p] : 0;  // issued with x
+  T xn[3] = {T(0), T(0), T(0)};
+  const bool moved = valid && g2p_particle(c, st, st_out, p, scene, grid, xn);
+  if (mark) {  // uniform; all lanes take part in the warp's writer election
+    Stencil<T> sn;
+    zero_stencil(sn);
+    const bool ok = moved && make_stencil(c, xn, sn);
+    mark_stencil_blocks(c, ok, sn.base, scene, mark);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      header[0] = 0;
+      header[1] = 0;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1211,11 +1272,9 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 5 : 
 //   its length, grid a (p2g) and grid a_out (grid_op output) come back from
 //   the store, and the same blocks of grid b (may be null) are zeroed;
 // - otherwise: the list length and the reservation ticket are reset, and
-//   flags[scene*NB3 + block] = 1 for every block a particle stencil touches.
-//   The flags are clean on entry (the compaction clears every flag it reads).
-//   In cell order neighbouring particles touch the same blocks, so a lane
-//   whose (scene, block range) equals the previous lane's writes nothing:
-//   about one flag store per block per warp instead of one per particle.
+//   flags[scene*NB3 + block] = 1 for every block a particle stencil touches
+//   (mark_stencil_blocks).  The flags are clean on entry (the compaction
+//   clears every flag it reads).
 // Grid-stride over warp-aligned ranges.
 template <typename T>
 __global__ void __launch_bounds__(256) k_mark_or_restore(Consts<T> c, const T* __restrict__ st,
@@ -1245,43 +1304,19 @@ __global__ void __launch_bounds__(256) k_mark_or_restore(Consts<T> c, const T* _
     header[0] = 0;  // list length (the compaction's append counter)
     header[1] = 0;  // reservation ticket
   }
-  const int lane = threadIdx.x & 31;
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p - lane < c.n_particles; p += stride) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p - (threadIdx.x & 31) < c.n_particles;
+       p += stride) {
     bool ok = false;
-    int scene = 0, lo[3] = {0, 0, 0}, ext[3] = {0, 0, 0};
-    unsigned long long key = ~0ull;
+    int scene = 0;
+    Stencil<T> s;
+    zero_stencil(s);
     if (p < c.n_particles) {
       T x[3];
       load_row(st, c.ld, p, 0, 3, x);
-      const int sc = pscene[p];  // issued with the x loads
-      Stencil<T> s;
+      scene = pscene[p];  // issued with the x loads
       ok = make_stencil(c, x, s);  // out-of-grid particles are skipped (and flagged) by the scatter
-      if (ok) {
-        scene = sc;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          lo[d] = s.base[d] >> 2;
-          ext[d] = ((s.base[d] + 2) >> 2) - lo[d];  // 0 or 1
-        }
-        // n_grid <= 1024: block coordinates fit 9 bits
-        key = ((unsigned long long)scene << 30) | ((unsigned long long)lo[0] << 21) |
-              ((unsigned long long)lo[1] << 12) | ((unsigned long long)lo[2] << 3) |
-              (unsigned long long)(ext[0] << 2 | ext[1] << 1 | ext[2]);
-      }
     }
-    const unsigned long long prev = __shfl_up_sync(0xffffffffu, key, 1);
-    if (ok && (lane == 0 || prev != key)) {
-      // the 1, 2, 4 or 8 blocks (lo + {0, ext}) as predicated stores; the
-      // offset within a scene fits 32 bits (nb <= 256)
-      unsigned char* f = flags + (int64_t)scene * c.NB3;
-      const int nb = c.nb;
-      const int i0 = (lo[0] * nb + lo[1]) * nb + lo[2];
-#pragma unroll
-      for (int m = 0; m < 8; ++m) {
-        const int di = m >> 2, dj = (m >> 1) & 1, dk = m & 1;
-        if (di <= ext[0] && dj <= ext[1] && dk <= ext[2]) f[i0 + (di * nb + dj) * nb + dk] = 1;
-      }
-    }
+    mark_stencil_blocks(c, ok, s.base, scene, flags);
   }
 }
 

@@ -80,9 +80,13 @@ inline size_t blockbuf_bytes(int64_t n_scenes, int n_grid) {
   return 16 + (size_t)(n_scenes * nb * nb * nb);
 }
 
+// premarked: the block flags of st0 were set by the previous substep's g2p
+// (chained substeps), so the marking pass is skipped; mark_next: this
+// substep's g2p flags the blocks of st1 for the next substep
 template <typename T, typename S>
 cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const double* pose_f,
-                               const double* pose_f1, const MpmGridStore* store = nullptr, int slot = -1);
+                               const double* pose_f1, const MpmGridStore* store = nullptr, int slot = -1,
+                               bool premarked = false, bool mark_next = false);
 template <typename T, typename S>
 cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* st1, const T* g1, T* g0, const double* pose_f,
                                const double* pose_f1, double* g_pose_f, double* g_pose_f1,

@@ -195,6 +195,13 @@ class MpmEngine:
                                                  _ptr(g_action), self.n_sub, _stream()), self.h,
                    "mpm_tools_action_bwd")
 
+    def set_chained(self, on: bool) -> None:
+        """Chained forward substeps (``mpm_set_chained``): each forward substep's
+        g2p flags the grid blocks of its output, and the next forward substep on
+        that frame skips its marking pass.  Only frames left unmodified between
+        substeps (up to the per-scene re-sort) may be chained."""
+        _lib.check(self.lib.mpm_set_chained(self.h, 1 if on else 0), self.h, "mpm_set_chained")
+
     def substep(self, st0, st1, pose_f, pose_f1, store: "GridStore" = None, slot: int = -1) -> None:
         if store is None:
             _lib.check(self.lib.mpm_substep_fwd(self.h, _ptr(st0), _ptr(st1), _ptr(pose_f), _ptr(pose_f1),
@@ -490,15 +497,21 @@ class Horizon:
         if store is not None:
             store.reset()
         cur = self.ckpt[0]
-        for f in range(self.F):
-            if (f + 1) % self.k == 0:
-                nxt = self.ckpt[(f + 1) // self.k]
-            else:
-                nxt = self.seg[(f + 1) % 2]
-            eng.substep(cur, nxt, self.pose[f], self.pose[f + 1], store, f)
-            if self.R and (f + 1) % self.R == 0 and f + 1 < self.F:
-                self._sort_frame(nxt, (f + 1) // self.R - 1)
-            cur = nxt
+        # each frame goes unmodified (up to the re-sort, a permutation within
+        # scenes) from one substep to the next: chain the substeps
+        eng.set_chained(True)
+        try:
+            for f in range(self.F):
+                if (f + 1) % self.k == 0:
+                    nxt = self.ckpt[(f + 1) // self.k]
+                else:
+                    nxt = self.seg[(f + 1) % 2]
+                eng.substep(cur, nxt, self.pose[f], self.pose[f + 1], store, f)
+                if self.R and (f + 1) % self.R == 0 and f + 1 < self.F:
+                    self._sort_frame(nxt, (f + 1) // self.R - 1)
+                cur = nxt
+        finally:
+            eng.set_chained(False)
 
     def loss(self, targets: torch.Tensor, density_weight: float = 1.0, contact_weight: float = 0.0,
              need_grad: bool = True) -> torch.Tensor:

@@ -187,6 +187,15 @@ int mpm_substep_bwd(MpmHandle* h, const void* state_f, const void* state_f1, con
                     void* g_state_f, const double* pose_f, const double* pose_f1, double* g_pose_f,
                     double* g_pose_f1, void* stream);
 
+/* Chained forward substeps (on = 1; off by default).  While on, each forward
+ * substep's g2p also flags the grid blocks of its output frame, and a forward
+ * substep whose input frame is the previous forward substep's output skips
+ * its own marking pass.  Contract: between two such substeps the frame is
+ * not modified, except by a permutation of the particles within their scene
+ * columns (the re-sort), which leaves the set of blocks unchanged.  Any
+ * adjoint substep ends the chain.  No counterpart in the reference. */
+int mpm_set_chained(MpmHandle* h, int32_t on);
+
 /* mpm_substep_fwd that also keeps the substep's forward grids in store slot
  * `slot` (no counterpart in the reference, whose substep_grad always
  * recomputes the grid, mpm_simulator.py:327-333). */

@@ -447,3 +447,25 @@ def test_config4_grid128_knife_gripper_trajectory(gpu_lib, prec, loss_tol, grad_
     assert abs(loss - ref_loss) / abs(ref_loss) < loss_tol, (loss, ref_loss)
     assert np.abs(ref_grad).max() > 0
     assert rel_err(grad, ref_grad) < grad_tol, (grad, ref_grad)
+
+
+@pytest.mark.gpu
+def test_chained_forward_equals_unchained(gpu_lib):
+    """Chained forward substeps (g2p flags the next substep's blocks, the
+    marking pass is skipped) give the frames of unchained substeps."""
+    sc = small_scene(n=4000, n_actions=2, substeps=30, tools=[all_tools()[1], all_tools()[2]], precision="fp64")
+    eng = make_engine(sc)
+    hz = Horizon(eng, sc.n_actions, ckpt_every=1, resort_every=0)  # keep the particle order
+    st0 = eng.init_state([sc.x0])
+    acts = eng.expand_actions([sc.actions])
+    hz.forward(st0, acts)  # chained inside
+    chained = hz.final.clone()
+    frames = [st0.clone(), eng.new_state()]
+    eng.set_chained(False)
+    for f in range(hz.F):
+        eng.substep(frames[f % 2], frames[(f + 1) % 2], hz.pose[f], hz.pose[f + 1])
+    plain = frames[hz.F % 2]
+    torch.cuda.synchronize()
+    P = eng.P
+    assert hz.R == 0
+    assert rel_err(chained[:, :P].cpu().numpy(), plain[:, :P].cpu().numpy()) < 1e-12
