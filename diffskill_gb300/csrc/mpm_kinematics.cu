@@ -367,7 +367,10 @@ __global__ void k_tools_action_bwd(const MpmToolDesc* __restrict__ tools, const 
       const double* p0 = pose + ((int64_t)s * n_tools + t) * 8;
       const double* vv = vel + ((int64_t)s * n_tools + t) * 8;
       const double* g1 = g_pose + ((int64_t)(s + 1) * n_tools + t) * 8;
-      double* g0 = g_pose + ((int64_t)s * n_tools + t) * 8;
+      // frame s gets this step's contribution by atomic adds: frame 0 of the
+      // action is also the last frame of the action before, whose MPM adjoint
+      // may be adding pose gradients to it at the same time
+      double g0[8] = {0, 0, 0, 0, 0, 0, 0, 0};
       double gvv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
       if (rolling_pin(d.type)) {
         rolling_fk_vjp(d, p0, vv, g1, g0, gvv);
@@ -381,6 +384,9 @@ __global__ void k_tools_action_bwd(const MpmToolDesc* __restrict__ tools, const 
         }
         fk_step_vjp(d, p0, vv, wq, g1, g0, gvv, gwq_run);
       }
+      double* gd = g_pose + ((int64_t)s * n_tools + t) * 8;
+      for (int k = 0; k < 8; ++k)
+        if (g0[k] != 0.0) atomicAdd(gd + k, g0[k]);
       for (int k = 0; k < 8; ++k) gvv_sum[k] += gvv[k];
     }
     __syncwarp();

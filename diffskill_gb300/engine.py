@@ -419,6 +419,9 @@ class Horizon:
         self.acts = torch.zeros((self.A, T, 8), dtype=torch.float64, device=dev)
         self.g_pose = torch.zeros_like(self.pose)
         self.g_act = torch.zeros_like(self.acts)
+        # the tool kinematics (one warp per scene, serial over substeps) run on
+        # a side stream, overlapped with the MPM substeps that do not need them
+        self.side = torch.cuda.Stream(device=dev)
         self.coll = eng.new_coll(self.A)
         self.g = torch.zeros((2, N_ROWS, eng.ld), dtype=dt, device=dev)
         self.gm = torch.zeros((eng.S, eng.G), dtype=dt, device=dev)
@@ -486,13 +489,22 @@ class Horizon:
     def forward(self, state0: torch.Tensor, actions: torch.Tensor, pose0: Optional[torch.Tensor] = None) -> None:
         """Run all actions: ``GradModel.forward_step`` for each action (function.py:166-175)."""
         eng, n = self.eng, self.eng.n_sub
+        main = torch.cuda.current_stream()
         self.ckpt[0].copy_(state0)
+        ready = []  # ready[s]: the poses of action s are computed
         if eng.T:
             self.pose[0].copy_(eng.pose0 if pose0 is None else pose0)
             self.acts.copy_(actions)
-            for s in range(self.A):
-                eng.tools_action(self.acts[s], self.vel[s * n], self.pose[s * n],
-                                 None if self.coll is None else self.coll[s])
+            # action s's kinematics run ahead on the side stream; the substeps of
+            # action s wait for them only
+            self.side.wait_stream(main)
+            with torch.cuda.stream(self.side):
+                for s in range(self.A):
+                    eng.tools_action(self.acts[s], self.vel[s * n], self.pose[s * n],
+                                     None if self.coll is None else self.coll[s])
+                    ev = torch.cuda.Event()
+                    ev.record(self.side)
+                    ready.append(ev)
         store = self.store if (self.store is not None and self.k == 1) else None
         if store is not None:
             store.reset()
@@ -502,6 +514,8 @@ class Horizon:
         eng.set_chained(True)
         try:
             for f in range(self.F):
+                if ready and f % n == 0:
+                    main.wait_event(ready[f // n])
                 if (f + 1) % self.k == 0:
                     nxt = self.ckpt[(f + 1) // self.k]
                 else:
@@ -512,6 +526,8 @@ class Horizon:
                 cur = nxt
         finally:
             eng.set_chained(False)
+        if ready:
+            main.wait_stream(self.side)
 
     def loss(self, targets: torch.Tensor, density_weight: float = 1.0, contact_weight: float = 0.0,
              need_grad: bool = True) -> torch.Tensor:
@@ -554,6 +570,29 @@ class Horizon:
         nxt = self.g[1]
         self.g_act.zero_()
         store = self.store
+        main = torch.cuda.current_stream()
+        if eng.T:
+            self.side.wait_stream(main)
+        pending = self.A - 1  # next action whose kinematics adjoint is due
+
+        def tools_bwd_upto(first_frame: int) -> None:
+            # every action whose substeps are all at or after first_frame has its
+            # MPM adjoint complete: its kinematics adjoint runs on the side stream,
+            # in descending action order, overlapped with the MPM adjoint of the
+            # earlier actions (the shared boundary frame takes atomic adds)
+            nonlocal pending
+            if not eng.T:
+                return
+            while pending >= 0 and pending * n >= first_frame:
+                ev = torch.cuda.Event()
+                ev.record(main)
+                self.side.wait_event(ev)
+                with torch.cuda.stream(self.side):
+                    s = pending
+                    eng.tools_action_bwd(self.vel[s * n], self.pose[s * n], self.g_pose[s * n], self.g_act[s],
+                                         None if self.coll is None else self.coll[s])
+                pending -= 1
+
         for c in range(self.F // k - 1, -1, -1):
             frames = [self.ckpt[c]]
             if store is not None and k > 1:
@@ -575,9 +614,9 @@ class Horizon:
             f0 = c * k
             if self.R and f0 > 0 and f0 % self.R == 0:
                 self._unsort_grad(cur, f0 // self.R - 1)
+            tools_bwd_upto(f0)
+        tools_bwd_upto(0)
         if eng.T:
-            for s in range(self.A - 1, -1, -1):
-                eng.tools_action_bwd(self.vel[s * n], self.pose[s * n], self.g_pose[s * n], self.g_act[s],
-                                     None if self.coll is None else self.coll[s])
+            main.wait_stream(self.side)
         self.g_state0 = cur
         return self.g_act
