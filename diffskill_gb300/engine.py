@@ -451,6 +451,7 @@ class Horizon:
         self.perms = torch.zeros((max(len(self.boundaries), 1), max(eng.P, 1)), dtype=torch.int64, device=dev)
         counts = torch.as_tensor(np.diff(eng.offsets), device=dev)
         self.pscene = torch.repeat_interleave(torch.arange(eng.S, device=dev), counts)
+        self.pscene32 = self.pscene.to(torch.int32)
         self._tmp = torch.empty((N_ROWS, max(eng.P, 1)), dtype=dt, device=dev)
 
     def bytes(self) -> int:
@@ -468,11 +469,13 @@ class Horizon:
         if P == 0:
             return
         n = eng.n_grid
-        base = (frame[0:3, :P] * n - 0.5).to(torch.int64).clamp_(0, n - 1)
         nb = n // 4
+        # 32-bit keys (half the radix-sort passes) whenever scene, block and cell fit
+        it = torch.int32 if eng.S * nb ** 3 * 64 < 2 ** 31 else torch.int64
+        base = (frame[0:3, :P] * n - 0.5).to(it).clamp_(0, n - 1)
         blk = ((base[0] >> 2) * nb + (base[1] >> 2)) * nb + (base[2] >> 2)
         loc = ((base[0] & 3) << 4) | ((base[1] & 3) << 2) | (base[2] & 3)
-        key = (self.pscene * (nb ** 3) + blk) * 64 + loc
+        key = ((self.pscene32 if it == torch.int32 else self.pscene) * (nb ** 3) + blk) * 64 + loc
         perm = torch.argsort(key)
         self.perms[b].copy_(perm)
         torch.index_select(frame[:, :P], 1, perm, out=self._tmp)
