@@ -274,8 +274,8 @@ def test_oracle_is_deterministic_across_thread_counts():
     assert np.array_equal(a, b) and np.array_equal(ga, gb)
 
 
-def test_baseline_config1_time_step_diverges():
-    """The benchmark definition's dt=5e-4 exceeds the CFL limit dx/c ~ 2.1e-4
+def test_single_scene_dt_5e4_exceeds_cfl_and_diverges():
+    """dt=5e-4 on the single-scene 64^3 workload exceeds the CFL limit dx/c ~ 2.1e-4
     (c = sqrt((lam+2mu)/rho) ~ 74.5): the FP64 oracle produces NaN; the
     reference's own dt=1e-4 (mpm_simulator.py:27) stays finite."""
     sc = scenes.config1(n_actions=4, n_particles=2000, dt=5e-4, substeps=50)
