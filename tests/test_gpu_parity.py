@@ -256,6 +256,25 @@ def test_out_of_grid_particle_sets_status_and_is_skipped(gpu_lib):
     assert np.allclose(got, [1.5, 0.5, 0.5])
 
 
+@pytest.mark.gpu
+def test_nonfinite_state_sets_status_and_raises(gpu_lib):
+    """A NaN in one particle's deformation gradient is reported through the
+    sticky status word (the kernels bound every loop and index, so nothing
+    faults), and check_status raises like the reference's NaN check."""
+    sc = small_scene(n=500, precision="fp32")
+    eng = make_engine(sc)
+    s0 = eng.init_state([sc.x0])
+    s0[15, 11] = float("nan")
+    s1 = eng.new_state()
+    pose = eng.pose0.unsqueeze(0).repeat(2, 1, 1).contiguous()
+    eng.substep(s0, s1, pose[0], pose[1])
+    torch.cuda.synchronize()
+    assert eng.status(clear=False) & 2
+    with pytest.raises(FloatingPointError):
+        eng.check_status()
+    assert eng.status(clear=True) == 0
+
+
 def test_invalid_arguments_raise(gpu_lib):
     from diffskill_gb300 import _lib
     sc = small_scene(n=100, precision="fp32")
