@@ -27,8 +27,9 @@ struct SvdIters<double> {
 };
 
 // rotation tangent t = sgn(theta) / (|theta| + sqrt(theta^2 + 1)) and cosine c;
-// FP32 uses the fast reciprocal and rsqrt (c and s = t c come from the same
-// rsqrt, so the rotation stays orthogonal to rounding)
+// FP32 uses the approximate reciprocal, square root and rsqrt: the error only
+// moves the rotation angle, and c and s = t c come from the same rsqrt, so the
+// rotation stays orthogonal to rounding
 MPM_DI void rot_tc(double theta, double& t, double& c) {
   t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
   c = 1.0 / sqrt(t * t + 1.0);
@@ -36,17 +37,25 @@ MPM_DI void rot_tc(double theta, double& t, double& c) {
 MPM_DI void rot_tc(float theta, float& t, float& c) {
   const float at = fabsf(theta);
   // for huge |theta|, t ~ 1/(2 theta) (avoids theta^2 overflow)
-  const float den = at < 1e18f ? at + sqrtf(fmaf(theta, theta, 1.0f)) : 2.0f * at;
-  t = copysignf(__frcp_rn(den), theta);
+  const float y = fmaf(theta, theta, 1.0f);
+  const float den = at < 1e18f ? at + y * rsqrtf(y) : 2.0f * at;
+  t = copysignf(__fdividef(1.0f, den), theta);
   c = rsqrtf(fmaf(t, t, 1.0f));
 }
+
+// a / b; FP32 by the approximate reciprocal (|b| < 2^126 here).  Used for the
+// Jacobi angle, and for the SVD backward's 1 / (s_j^2 - s_i^2), whose divisor
+// is clamped to |b| >= 1e-6.  The substep kernels are built with -ftz=true, so
+// a subnormal s_pq compares equal to 0 and is never a divisor.
+MPM_DI double fast_div(double a, double b) { return a / b; }
+MPM_DI float fast_div(float a, float b) { return __fdividef(a, b); }
 
 // one Jacobi rotation zeroing s_pq of the symmetric matrix held as
 // (s_pp, s_qq, s_pq, s_rp, s_rq); V columns p, q rotated alongside
 template <typename T>
 MPM_DI void jacobi_rot(T& app, T& aqq, T& apq, T& arp, T& arq, T* V, int p, int q) {
   if (apq == T(0)) return;
-  T theta = (aqq - app) / (T(2) * apq);
+  T theta = fast_div(aqq - app, T(2) * apq);
   T t, c;
   rot_tc(theta, t, c);
   T s = t * c;
@@ -167,7 +176,7 @@ MPM_DI void svd3_bwd(const T* U, const T* s, const T* V, const T* gU, const T* g
       if (i == j) {
         X[i * 3 + j] = gs[i];
       } else {
-        T Fij = T(1) / svd_clamp(ss[j] - ss[i]);
+        T Fij = fast_div(T(1), svd_clamp(ss[j] - ss[i]));
         T au = UtgU[i * 3 + j] - UtgU[j * 3 + i];  // (U^T gU - gU^T U)_ij
         T av = VtgV[i * 3 + j] - VtgV[j * 3 + i];
         X[i * 3 + j] = Fij * (au * s[j] + s[i] * av);
