@@ -17,9 +17,13 @@ namespace mpm {
 
 MPM_DI float msqrt(float x) { return sqrtf(x); }
 MPM_DI double msqrt(double x) { return sqrt(x); }
-MPM_DI float mexp(float x) { return expf(x); }
+// FP32 exp and log by the hardware approximations (__expf, __logf): they
+// serve the return map's log/exp of singular values near 1 and the contact
+// softness exp(-dist * softness), where their error stays below the FP32
+// substep's own rounding noise
+MPM_DI float mexp(float x) { return __expf(x); }
 MPM_DI double mexp(double x) { return exp(x); }
-MPM_DI float mlog(float x) { return logf(x); }
+MPM_DI float mlog(float x) { return __logf(x); }
 MPM_DI double mlog(double x) { return log(x); }
 MPM_DI float msin(float x) { return sinf(x); }
 MPM_DI double msin(double x) { return sin(x); }
@@ -211,10 +215,11 @@ MPM_DI void qmul_raw(const T* q, const T* r, T* o) {
   o[2] = r[0] * q[2] + r[1] * q[3] + r[2] * q[0] - r[3] * q[1];
   o[3] = r[0] * q[3] - r[1] * q[2] + r[2] * q[1] + r[3] * q[0];
 }
-// 1 / sqrt(L2): FP64 through rsqrt (within 1 ulp; FP64 divide and square root
-// are long instruction sequences on GB300's FP64 pipe), FP32 as 1 / sqrtf
+// 1 / sqrt(L2) through rsqrt: FP64 within 1 ulp (FP64 divide and square root
+// are long instruction sequences on GB300's FP64 pipe), FP32 by the hardware
+// approximation
 MPM_DI double inv_len(double L2) { return rsqrt(L2); }
-MPM_DI float inv_len(float L2) { return 1.0f / sqrtf(L2); }
+MPM_DI float inv_len(float L2) { return rsqrtf(L2); }
 template <typename T>
 MPM_DI void qmul(const T* q, const T* r, T* out) {
   T o[4];

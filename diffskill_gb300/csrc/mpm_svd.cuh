@@ -116,9 +116,12 @@ MPM_DI void svd3(const T* A, T* U, T* s, T* V) {
   mm(A, V, B);
   T b0[3] = {B[0], B[3], B[6]}, b1[3] = {B[1], B[4], B[7]}, b2[3] = {B[2], B[5], B[8]};
   T u0[3], u1[3], u2[3];
-  T n0 = msqrt(dot3(b0, b0));
-  if (n0 > T(0)) {
-    T inv = T(1) / n0;
+  // column norms from one reciprocal square root each: |b| = b.b / sqrt(b.b)
+  T d0 = dot3(b0, b0);
+  T n0 = T(0);
+  if (d0 > T(0)) {
+    T inv = inv_len(d0);
+    n0 = d0 * inv;
 #pragma unroll
     for (int k = 0; k < 3; ++k) u0[k] = b0[k] * inv;
   } else {
@@ -126,9 +129,9 @@ MPM_DI void svd3(const T* A, T* U, T* s, T* V) {
   }
   T pr = dot3(u0, b1);
   T r1[3] = {b1[0] - pr * u0[0], b1[1] - pr * u0[1], b1[2] - pr * u0[2]};
-  T n1 = msqrt(dot3(r1, r1));
-  if (n1 > T(0)) {
-    T inv = T(1) / n1;
+  T d1 = dot3(r1, r1);
+  if (d1 > T(0)) {
+    T inv = inv_len(d1);
 #pragma unroll
     for (int k = 0; k < 3; ++k) u1[k] = r1[k] * inv;
   } else {
