@@ -315,14 +315,14 @@ MPM_DI void p2g_particle(const MatConsts<S>& m, const S* C, const S* F, P2G<S>& 
     P.sigc[i] = (S(0.05) < P.s[i]) ? P.s[i] : S(0.05);
     eps[i] = mlog(P.sigc[i]);
   }
-  S mean = (eps[0] + eps[1] + eps[2]) / S(3);
+  S mean = fast_div(eps[0] + eps[1] + eps[2], S(3));
 #pragma unroll
   for (int i = 0; i < 3; ++i) P.ehat[i] = eps[i] - mean;
   P.nrm = msqrt(dot3(P.ehat, P.ehat) + S(1e-8));
-  P.dg = P.nrm - m.ys / (S(2) * m.mu);
+  P.dg = P.nrm - fast_div(m.ys, S(2) * m.mu);
   P.yield = P.dg > S(0);
   if (P.yield) {
-    P.k = P.dg / P.nrm;
+    P.k = fast_div(P.dg, P.nrm);
 #pragma unroll
     for (int i = 0; i < 3; ++i) P.e[i] = mexp(eps[i] - P.k * P.ehat[i]);
     S UD[9];
@@ -397,14 +397,14 @@ MPM_DI void p2g_particle_vjp(const MatConsts<S>& m, const S* C, const S* F, cons
       g_k -= g_eps2[i] * P.ehat[i];
       g_ehat[i] = -P.k * g_eps2[i];
     }
-    S g_nrm = -g_k * P.dg / (P.nrm * P.nrm) + g_k / P.nrm;
+    S g_nrm = -fast_div(g_k * P.dg, P.nrm * P.nrm) + fast_div(g_k, P.nrm);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) g_ehat[i] += g_nrm * P.ehat[i] / P.nrm;
-    S sh = (g_ehat[0] + g_ehat[1] + g_ehat[2]) / S(3);
+    for (int i = 0; i < 3; ++i) g_ehat[i] += fast_div(g_nrm * P.ehat[i], P.nrm);
+    S sh = fast_div(g_ehat[0] + g_ehat[1] + g_ehat[2], S(3));
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       g_eps[i] += g_ehat[i] - sh;
-      gs[i] = (S(0.05) < P.s[i]) ? g_eps[i] / P.sigc[i] : S(0);
+      gs[i] = (S(0.05) < P.s[i]) ? fast_div(g_eps[i], P.sigc[i]) : S(0);
     }
 #pragma unroll
     for (int i = 0; i < 9; ++i) g_Ftmp[i] = S(0);
