@@ -82,15 +82,16 @@ def make_workload(name: str, rank: int, precision: str = "fp32"):
 def choose_checkpoint(scs, budget_frac: float = 0.5) -> int:
     """Smallest checkpoint interval (dividing the horizon) whose stored frames fit the budget."""
     import torch
+    from diffskill_gb300.engine import plan_checkpoint_interval
     P = sum(sc.n_particles for sc in scs)
     F = scs[0].n_actions * scs[0].sim.n_substeps
     w = 8 if scs[0].sim.precision_code == 2 else 4
     frame = 24 * (-(-P // 32) * 32) * w
     free, _ = torch.cuda.mem_get_info()
-    for k in (1, 2, 5, 10, 25, 50, 100):
-        if F % k == 0 and (F // k + 1 + k) * frame <= budget_frac * free:
-            return k
-    return scs[0].sim.n_substeps
+    try:
+        return plan_checkpoint_interval(F, frame, int(budget_frac * free))
+    except MemoryError:
+        return scs[0].sim.n_substeps
 
 
 # ----------------------------------------------------------------------------

@@ -15,7 +15,7 @@ This replaces the reference's store-every-frame fields (x, v, C, F of shape
 from __future__ import annotations
 
 import ctypes
-from typing import List, Optional, Sequence
+from typing import List, Optional, Sequence, Union
 
 import numpy as np
 import torch
@@ -385,12 +385,44 @@ class GridStore:
         return int((self.slot_start >= 0).sum())
 
 
+def horizon_frames(n_frames: int, k: int) -> int:
+    """State frames a horizon of ``n_frames`` substeps holds at checkpoint interval ``k``:
+    the checkpoints (``n_frames / k + 1``) and the recompute segment (``max(k, 2)``)."""
+    return n_frames // k + 1 + max(k, 2)
+
+
+def plan_checkpoint_interval(n_frames: int, frame_bytes: int, budget_bytes: int, fixed_bytes: int = 0) -> int:
+    """Checkpoint interval for a horizon of ``n_frames`` substeps under a memory budget.
+
+    The reference stores every frame (``max_steps`` frames of every field,
+    mpm_simulator.py:40-43) or, in its long-horizon notebook, checkpoints at a
+    hand-picked interval and recomputes (plb/optimizer/long_term_gradient.ipynb,
+    cell 4).  Here the interval is chosen: at interval k the adjoint recomputes
+    (k - 1) / k of the forward substeps, so the smallest divisor k of the
+    horizon whose frames (``horizon_frames``) fit ``budget_bytes - fixed_bytes``
+    is the fastest.  Raises ``MemoryError`` when no divisor fits.
+    """
+    if n_frames <= 0 or frame_bytes < 0:
+        raise ValueError("the horizon needs at least one substep and a non-negative frame size")
+    room = budget_bytes - fixed_bytes
+    for k in range(1, n_frames + 1):
+        if n_frames % k == 0 and horizon_frames(n_frames, k) * frame_bytes <= room:
+            return k
+    best = min((horizon_frames(n_frames, k), k) for k in range(1, n_frames + 1) if n_frames % k == 0)
+    raise MemoryError(f"a horizon of {n_frames} substeps needs at least {best[0]} frames of {frame_bytes} B "
+                      f"(interval {best[1]}), above the budget of {room} B")
+
+
 class Horizon:
     """Device buffers and the forward/backward sweep over ``n_actions`` actions.
 
     ``ckpt_every`` = k: the state is kept every k substeps (k=1 keeps every
     frame, as the reference does); the backward pass recomputes each segment
     of k substeps from its checkpoint before running its adjoint.
+    ``ckpt_every="auto"`` takes the smallest k whose frames fit
+    ``frame_budget_bytes`` (default: 60 % of the free device memory; the grid
+    store then takes a quarter of what is left), see
+    ``plan_checkpoint_interval``.
 
     ``resort_every`` = R (a multiple of k; default one action rounded up to a
     multiple of k, 0 = never): at every R-th frame the particles of each scene
@@ -400,11 +432,18 @@ class Horizon:
     gradients do not depend on the particle order.
     """
 
-    def __init__(self, eng: MpmEngine, n_actions: int, ckpt_every: int = 10, store_grids: bool = True,
-                 store_budget_bytes: Optional[int] = None, resort_every: Optional[int] = None):
+    def __init__(self, eng: MpmEngine, n_actions: int, ckpt_every: Union[int, str] = 10, store_grids: bool = True,
+                 store_budget_bytes: Optional[int] = None, resort_every: Optional[int] = None,
+                 frame_budget_bytes: Optional[int] = None):
         self.eng = eng
         self.A = int(n_actions)
         self.F = self.A * eng.n_sub
+        if ckpt_every == "auto":
+            if frame_budget_bytes is None:
+                free, _ = torch.cuda.mem_get_info(eng.device)
+                frame_budget_bytes = int(free * 0.6)
+            frame_bytes = N_ROWS * eng.ld * (8 if eng.dtype == torch.float64 else 4)
+            ckpt_every = plan_checkpoint_interval(self.F, frame_bytes, frame_budget_bytes)
         k = int(ckpt_every) if ckpt_every else eng.n_sub
         if self.F % k != 0:
             raise ValueError(f"checkpoint interval {k} must divide the horizon of {self.F} substeps")

@@ -18,7 +18,7 @@ Workloads (sizes from the project's benchmark definitions):
 from __future__ import annotations
 
 from dataclasses import dataclass, field
-from typing import List, Optional
+from typing import List, Optional, Union
 
 import numpy as np
 
@@ -35,7 +35,7 @@ class Scene:
     softness: float = 666.0
     density_weight: float = 1.0
     contact_weight: float = 0.0     # soft tool-contact term (loss.py:143-167)
-    checkpoint_every: int = 10
+    checkpoint_every: Union[int, str] = 10  # "auto": planned from the free device memory
     name: str = ""
 
     @property
@@ -244,5 +244,5 @@ def config5(n_scenes: int = 16, n_actions: int = 100, substeps: int = 50, dt: Op
         adim = action_dims(tools)[-1]
         actions = rng.uniform(-1, 1, size=(n_actions, adim))
         target = density_grid(clip_particles(x0 + np.array([0.1, 0.0, 0.0]), sim), sim.grid, sim.p_mass)
-        scenes.append(Scene(sim, tools, x0, target, actions, checkpoint_every=0, name=f"config5[{s}]"))
+        scenes.append(Scene(sim, tools, x0, target, actions, checkpoint_every="auto", name=f"config5[{s}]"))
     return scenes

@@ -10,7 +10,7 @@ allocation after the first call.
 """
 from __future__ import annotations
 
-from typing import List, Optional, Sequence
+from typing import List, Optional, Sequence, Union
 
 import numpy as np
 import torch
@@ -43,7 +43,7 @@ def _check_compatible(scenes: Sequence[Scene]) -> None:
 
 
 class BatchedTrajectory:
-    def __init__(self, scenes: Sequence[Scene], ckpt_every: Optional[int] = None, lr: float = 0.01,
+    def __init__(self, scenes: Sequence[Scene], ckpt_every: Union[int, str, None] = None, lr: float = 0.01,
                  betas=(0.9, 0.999), eps: float = 1e-8, softness: float = 666.0, sort_particles: bool = True):
         scenes = list(scenes)
         _check_compatible(scenes)

@@ -155,3 +155,36 @@ def test_scene_sharding_two_ranks_gloo():
     for rank, cover, load in out:
         assert cover == [1] * len(ns)
         assert load == max(sum(ns[i] for i in shard_scenes(ns, 2, r)) for r in range(2))
+
+
+def test_checkpoint_planner_picks_smallest_interval_that_fits():
+    """The interval planner of long horizons: store every frame when it fits,
+    else the smallest divisor of the horizon whose frames fit the budget."""
+    from diffskill_gb300.engine import horizon_frames, plan_checkpoint_interval
+    fb = 100
+    # everything fits: every frame is kept, as the reference does
+    assert plan_checkpoint_interval(1000, fb, 10 ** 9) == 1
+    assert horizon_frames(1000, 1) == 1003
+    # one byte short of store-all: the next divisor that fits
+    k = plan_checkpoint_interval(1000, fb, horizon_frames(1000, 1) * fb - 1)
+    assert k == 2 and 1000 % k == 0
+    # the chosen interval always fits, and every smaller divisor does not
+    for budget in (600 * fb, 200 * fb, 80 * fb, 70 * fb):
+        k = plan_checkpoint_interval(1000, fb, budget)
+        assert 1000 % k == 0 and horizon_frames(1000, k) * fb <= budget
+        for j in range(1, k):
+            assert 1000 % j or horizon_frames(1000, j) * fb > budget
+    # the fixed share comes off the budget
+    assert plan_checkpoint_interval(1000, fb, 10 ** 9, fixed_bytes=10 ** 9 - 600 * fb) > 1
+    # config 5 shapes: 100 actions x 50 substeps, 384 MiB frames, 189 GiB for frames
+    assert plan_checkpoint_interval(5000, 384 << 20, 189 << 30) == 20
+    # below the minimum (near sqrt of the horizon) no interval fits
+    with pytest.raises(MemoryError):
+        plan_checkpoint_interval(1000, fb, 60 * fb)
+    with pytest.raises(ValueError):
+        plan_checkpoint_interval(0, fb, 10 ** 9)
+
+
+def test_config5_asks_for_a_planned_interval():
+    sc = scenes.config5(n_scenes=2, n_actions=2, n_min=1000, n_max=2000)
+    assert all(s.checkpoint_every == "auto" for s in sc)
