@@ -188,3 +188,17 @@ def test_checkpoint_planner_picks_smallest_interval_that_fits():
 def test_config5_asks_for_a_planned_interval():
     sc = scenes.config5(n_scenes=2, n_actions=2, n_min=1000, n_max=2000)
     assert all(s.checkpoint_every == "auto" for s in sc)
+
+
+def test_build_flags_keep_the_renderer_exact():
+    """The substep units take the fast FP32 divide/sqrt and flush-to-zero; the
+    renderer keeps IEEE rounding without FMA contraction (its parity with the
+    oracle's restatement is bit-level)."""
+    from diffskill_gb300 import build
+    render = build.EXTRA["mpm_render.cu"]
+    assert "-fmad=false" in render
+    assert not any(f.startswith(("-prec-", "-ftz", "-use_fast_math")) for f in render)
+    for src in ("mpm_fwd.cu", "mpm_bwd.cu", "mpm_static.cu"):
+        assert {"-ftz=true", "-prec-div=false", "-prec-sqrt=false"} <= set(build.EXTRA[src])
+    for src in build.SOURCES:
+        assert "-use_fast_math" not in build.EXTRA.get(src, ())
