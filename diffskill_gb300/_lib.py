@@ -12,7 +12,7 @@ from typing import Optional
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmpm_gb300.so")
 
-ABI_VERSION = 3
+ABI_VERSION = 4
 MPM_OK = 0
 STATUS_OUT_OF_GRID = 1
 STATUS_NONFINITE = 2
@@ -54,6 +54,10 @@ class MpmRenderView(ctypes.Structure):
                 ("bias", ctypes.c_float * 2), ("sdf_threshold", ctypes.c_float), ("show_particles", _i32)]
 
 
+class MpmTuning(ctypes.Structure):
+    _fields_ = [("p2g_ctas", _i32), ("g2p_adj_ctas", _i32), ("p2g_adj_ctas", _i32), ("grid_ctas_per_sm", _i32)]
+
+
 class MpmGridStore(ctypes.Structure):
     _fields_ = [("blocks", _c_p), ("block_ids", _c_p), ("slot_start", _c_p), ("slot_count", _c_p), ("bump", _c_p),
                 ("capacity", _i64), ("n_slots", _i32), ("reserved", _i32)]
@@ -70,6 +74,8 @@ SIGNATURES = {
     "mpm_tools_action": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _i32, _c_p]),
     "mpm_tools_action_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _i32, _c_p]),
     "mpm_set_chained": (_i32, [_c_p, _i32]),
+    "mpm_set_tuning": (_i32, [_c_p, ctypes.POINTER(MpmTuning)]),
+    "mpm_get_tuning": (_i32, [_c_p, ctypes.POINTER(MpmTuning)]),
     "mpm_substep_fwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_substep_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_substep_fwd_store": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, ctypes.POINTER(MpmGridStore), _i32, _c_p]),
@@ -92,7 +98,7 @@ SIGNATURES = {
     "mpm_tool_distance": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_tool_distance_bwd": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "mpm_substep_fwd_static": (_i32, [ctypes.POINTER(MpmParams), ctypes.POINTER(MpmToolDesc), _i32, _c_p, _c_p, _c_p,
-                                      _c_p, _c_p]),
+                                      _c_p, _c_p, _c_p]),
     "mpm_status": (_i32, [_c_p, ctypes.POINTER(ctypes.c_uint32), _i32, _c_p]),
     "mpm_last_error": (_i32, [_c_p, ctypes.c_char_p, ctypes.c_size_t]),
     "mpm_launch_count": (_i64, [_c_p]),

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <initializer_list>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -24,6 +25,7 @@ struct MpmHandle {
   MpmToolDesc* d_tools = nullptr;
   int n_tools = 0;
   bool chained = false;           // mpm_set_chained
+  MpmTuning tune = {0, 0, 0, 0};  // mpm_set_tuning
   const void* premarked = nullptr;  // frame whose block flags the last forward g2p set
   std::vector<MpmToolDesc> h_tools;
   unsigned int* d_status = nullptr;
@@ -113,6 +115,7 @@ mpm::LaunchCtx ctx(MpmHandle* h, void* stream) {
   L.stream = (cudaStream_t)stream;
   L.launches = &h->launches;
   L.prof = &h->prof;
+  L.tune = h->tune;
   return L;
 }
 int check_device(MpmHandle* h) {
@@ -460,6 +463,35 @@ int mpm_set_chained(MpmHandle* h, int32_t on) {
   if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_set_chained: NULL handle");
   h->chained = on != 0;
   h->premarked = nullptr;
+  return MPM_OK;
+}
+
+int mpm_set_tuning(MpmHandle* h, const MpmTuning* t) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_set_tuning: NULL handle");
+  if (!t) return fail(h, MPM_E_INVALID, "mpm_set_tuning: NULL tuning");
+  auto in = [](int v, std::initializer_list<int> ok) {
+    for (int o : ok)
+      if (v == o) return true;
+    return false;
+  };
+  if (!in(t->p2g_ctas, {0, 6, 7, 8})) return fail(h, MPM_E_INVALID, "mpm_set_tuning: p2g_ctas must be 0, 6, 7 or 8");
+  if (!in(t->g2p_adj_ctas, {0, 5, 6, 7, 8}))
+    return fail(h, MPM_E_INVALID, "mpm_set_tuning: g2p_adj_ctas must be 0, 5, 6, 7 or 8");
+  if (!in(t->p2g_adj_ctas, {0, 4, 5, 6}))
+    return fail(h, MPM_E_INVALID, "mpm_set_tuning: p2g_adj_ctas must be 0, 4, 5 or 6");
+  if (t->grid_ctas_per_sm != 0 && (t->grid_ctas_per_sm < 2 || t->grid_ctas_per_sm > 64))
+    return fail(h, MPM_E_INVALID, "mpm_set_tuning: grid_ctas_per_sm must be 0 or in [2, 64]");
+  h->tune = *t;
+  return MPM_OK;
+}
+
+int mpm_get_tuning(MpmHandle* h, MpmTuning* t) {
+  if (!h || !t) return fail(h, MPM_E_INVALID, "mpm_get_tuning: NULL argument");
+  *t = h->tune;
+  if (!t->p2g_ctas) t->p2g_ctas = 7;
+  if (!t->g2p_adj_ctas) t->g2p_adj_ctas = 6;
+  if (!t->p2g_adj_ctas) t->p2g_adj_ctas = 5;
+  if (!t->grid_ctas_per_sm) t->grid_ctas_per_sm = 16;
   return MPM_OK;
 }
 

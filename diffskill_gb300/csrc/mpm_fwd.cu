@@ -95,7 +95,8 @@ cudaError_t convert_tools(int precision, int n, const MpmToolDesc* tools, void* 
 }
 
 unsigned grid_blocks_launch(const LaunchCtx& L, int64_t total_blocks) {
-  int64_t g = (int64_t)L.sm_count * 16;
+  const int per_sm = L.tune.grid_ctas_per_sm > 0 ? L.tune.grid_ctas_per_sm : 16;
+  int64_t g = (int64_t)L.sm_count * per_sm;
   return (unsigned)(g < total_blocks ? g : (total_blocks > 0 ? total_blocks : 1));
 }
 
@@ -110,9 +111,23 @@ cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const d
   cudaError_t e = prepare_blocks<T>(L, c, st0, gin, (Node<T>*)nullptr, (Node<T>*)nullptr, nullptr, -1, store, slot,
                                     pose_f, pose_f1, premarked);
   if (e != cudaSuccess) return e;
-  if (c.n_particles > 0)
-    MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S>), blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gin,
-               (const int64_t*)nullptr);
+  if (c.n_particles > 0) {
+    const unsigned pb = blocks_for(c.n_particles, 128);
+    const int64_t* none = nullptr;
+    // FP32: the CTAs-per-SM variant the tuning selects
+    const int v = L.tune.p2g_ctas;
+    if constexpr (sizeof(T) == 4 && sizeof(S) == 4) {
+      if (v == 6)
+        MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S, false, 6>), pb, 128, c, st0, st1, L.pscene, gin, none);
+      else if (v == 8)
+        MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S, false, 8>), pb, 128, c, st0, st1, L.pscene, gin, none);
+      else
+        MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S>), pb, 128, c, st0, st1, L.pscene, gin, none);
+    } else {
+      (void)v;
+      MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S>), pb, 128, c, st0, st1, L.pscene, gin, none);
+    }
+  }
   MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3), 64, c, L.active,
              counter, gin, gout, (const Tool<T>*)L.tools_t, (const T*)L.poses_t, L.tool_off,
              store ? *store : MpmGridStore{}, store ? slot : -1, (const int64_t*)nullptr);

@@ -293,74 +293,278 @@ MPM_DI void store_row(T* __restrict__ st, int64_t ld, int64_t p, int r0, int n, 
 // ---------------------------------------------------------------------------
 template <typename S>
 struct P2G {
-  S Ftmp[9], U[9], s[3], V[9];
+  S U[9], s[3], V[9];
+  S sm1[3];  // s - 1 (FP32: from the shifted SVD, exact as s -> 1)
   S sigc[3], ehat[3], nrm, dg, k, e[3];
   bool yield;
   S newF[9], J, R[9];
+  S em1[3];  // singular values of newF minus 1 (e - 1 when yielding, else s - 1)
+  S A[9];    // newF - R (FP32: U diag(e - 1) V^T, no cancellation)
 };
 template <typename S>
 struct MatConsts {
   S dt, mu, lam, ys, ks, p_mass;
 };
+// affine = ks (2 mu A newF^T + lam J (J - 1) I) + p_mass C (mpm_simulator.py:213-215)
 template <typename S>
-MPM_DI void p2g_particle(const MatConsts<S>& m, const S* C, const S* F, P2G<S>& P, S* affine) {
-  S IC[9];
-#pragma unroll
-  for (int i = 0; i < 9; ++i) IC[i] = m.dt * C[i] + ((i % 4 == 0) ? S(1) : S(0));
-  mm(IC, F, P.Ftmp);
-  svd3(P.Ftmp, P.U, P.s, P.V);
-  S eps[3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    P.sigc[i] = (S(0.05) < P.s[i]) ? P.s[i] : S(0.05);
-    eps[i] = mlog(P.sigc[i]);
-  }
-  S mean = fast_div(eps[0] + eps[1] + eps[2], S(3));
-#pragma unroll
-  for (int i = 0; i < 3; ++i) P.ehat[i] = eps[i] - mean;
-  P.nrm = msqrt(dot3(P.ehat, P.ehat) + S(1e-8));
-  P.dg = P.nrm - fast_div(m.ys, S(2) * m.mu);
-  P.yield = P.dg > S(0);
-  if (P.yield) {
-    P.k = fast_div(P.dg, P.nrm);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) P.e[i] = mexp(eps[i] - P.k * P.ehat[i]);
-    S UD[9];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int cc = 0; cc < 3; ++cc) UD[r * 3 + cc] = P.U[r * 3 + cc] * P.e[cc];
-    mmT(UD, P.V, P.newF);
-  } else {
-    P.k = S(0);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) P.e[i] = S(1);
-#pragma unroll
-    for (int i = 0; i < 9; ++i) P.newF[i] = P.Ftmp[i];
-  }
-  P.J = det3(P.newF);
-  mmT(P.U, P.V, P.R);
-  S A[9], st[9];
-#pragma unroll
-  for (int i = 0; i < 9; ++i) A[i] = P.newF[i] - P.R[i];
-  mmT(A, P.newF, st);
+MPM_DI void p2g_affine(const MatConsts<S>& m, const P2G<S>& P, S Jm1, const S* C, S* affine) {
+  S st[9];
+  mmT(P.A, P.newF, st);
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
     S v = S(2) * m.mu * st[i];
-    if (i % 4 == 0) v += m.lam * P.J * (P.J - S(1));
+    if (i % 4 == 0) v += m.lam * P.J * Jm1;
     affine[i] = m.ks * v + m.p_mass * C[i];
   }
 }
-// adjoint; g_C, g_F are written (not accumulated)
+// FP32 p2g math in terms of the displacement D = F_tmp - I.  The stress
+// 2 mu (newF - R) newF^T + lam J (J - 1) I is a difference of numbers near 1
+// (newF, R, J) when it is evaluated as written; in FP32 that cancellation
+// leaves about 1e-7 / |strain| of relative error in every particle's stress
+// (1e-4 at a strain of 1e-3), which then drives the trajectory apart from the
+// FP64 one.  Here every small quantity is formed directly: D = G + dt C (I + G)
+// with G = F - I (exact for F_ii in [0.5, 2]); the SVD of I + D from the
+// shifted matrix (svd3_shifted) with s - 1; log(s) = log1p(s - 1); the
+// projected singular values e - 1 = expm1(eps'); newF - R = U diag(e - 1) V^T;
+// J - 1 = det(I + D) - 1 = tr D + (tr(D)^2 - tr(D^2)) / 2 + det D (elastic) or
+// expm1(sum eps) (yield: the von Mises map keeps the volume).  The stored F
+// of a yielding particle is formed as I + (D + U diag(e - s) V^T), its
+// plastic correction e - s = s expm1(-k eps_hat) taken without cancellation,
+// so it carries one FP32 rounding, as an elastic particle's I + D does.
+// Mathematically the same function as the reference's (mpm_simulator.py:
+// 122-129, 166-225).  The stress takes the SVD basis,
+// (newF - R) newF^T = U diag((e - 1) e) U^T; new_F (may be null: the
+// adjoint's recompute) receives the updated F.
+MPM_DI void p2g_particle_f32(const MatConsts<float>& m, const float* C, const float* F, P2G<float>& P,
+                             float* affine, float* new_F) {
+  float G[9], CG[9], D[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) G[i] = F[i] - ((i % 4 == 0) ? 1.f : 0.f);
+  mm(C, G, CG);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) D[i] = G[i] + m.dt * (C[i] + CG[i]);
+  svd3_shifted(D, P.U, P.s, P.sm1, P.V);
+  float eps[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const bool above = 0.05f < P.s[i];
+    P.sigc[i] = above ? P.s[i] : 0.05f;
+    eps[i] = above ? log1p_strain(P.sm1[i]) : logf(0.05f);
+  }
+  const float esum = eps[0] + eps[1] + eps[2];
+  const float mean = fast_div(esum, 3.f);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) P.ehat[i] = eps[i] - mean;
+  P.nrm = sqrtf(dot3(P.ehat, P.ehat) + 1e-8f);
+  P.dg = P.nrm - fast_div(m.ys, 2.f * m.mu);
+  P.yield = P.dg > 0.f;
+  float* em1 = P.em1;
+  float pc[3];  // e - s, the return map's change of the singular values
+  if (P.yield) {
+    P.k = fast_div(P.dg, P.nrm);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      em1[i] = expm1_strain(eps[i] - P.k * P.ehat[i]);
+      P.e[i] = 1.f + em1[i];
+      // both small and accurate to ~1e-7 of themselves: the difference keeps that accuracy
+      pc[i] = 0.05f < P.s[i] ? em1[i] - P.sm1[i] : P.e[i] - P.s[i];
+    }
+  } else {
+    P.k = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      P.e[i] = 1.f;
+      em1[i] = P.sm1[i];
+      pc[i] = 0.f;
+    }
+  }
+  // J - 1: det(I + D) - 1 by its invariants; the return map keeps the volume,
+  // unless a singular value sits at the 0.05 floor (then J = prod sigc)
+  float Jm1;
+  if (P.yield && !(0.05f < P.s[0] && 0.05f < P.s[1] && 0.05f < P.s[2])) {
+    Jm1 = expm1f(esum);
+  } else {
+    const float tr = D[0] + D[4] + D[8];
+    float D2 = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) D2 += D[i * 3 + j] * D[j * 3 + i];
+    Jm1 = tr + 0.5f * (tr * tr - D2) + det3(D);
+  }
+  P.J = 1.f + Jm1;
+  // (newF - R) newF^T = U diag(e - 1) V^T V diag(e) U^T = U diag((e - 1) e) U^T
+  float h[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) h[i] = em1[i] * (1.f + em1[i]);
+  const float lj = m.lam * P.J * Jm1;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = i; j < 3; ++j) {
+      float st = P.U[i * 3] * P.U[j * 3] * h[0] + P.U[i * 3 + 1] * P.U[j * 3 + 1] * h[1] +
+                 P.U[i * 3 + 2] * P.U[j * 3 + 2] * h[2];
+      st = 2.f * m.mu * st + (i == j ? lj : 0.f);
+      affine[i * 3 + j] = m.ks * st + m.p_mass * C[i * 3 + j];
+      if (j != i) affine[j * 3 + i] = m.ks * st + m.p_mass * C[j * 3 + i];
+    }
+  if (new_F) {
+    if (P.yield) {
+      float UP[9], corr[9];
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) UP[r * 3 + cc] = P.U[r * 3 + cc] * pc[cc];
+      mmT(UP, P.V, corr);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) new_F[i] = (D[i] + corr[i]) + ((i % 4 == 0) ? 1.f : 0.f);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 9; ++i) new_F[i] = D[i] + ((i % 4 == 0) ? 1.f : 0.f);  // F_tmp
+    }
+  }
+}
+// affine (the APIC matrix with the stress) and, when new_F is given, the
+// updated F; P keeps what the adjoint needs
 template <typename S>
-MPM_DI void p2g_particle_vjp(const MatConsts<S>& m, const S* C, const S* F, const P2G<S>& P, const S* g_affine,
-                             const S* g_newF_in, S* g_C, S* g_F) {
-  S g_raw[9], A[9], tmp[9], g_newF[9], g_R[9];
+MPM_DI void p2g_particle(const MatConsts<S>& m, const S* C, const S* F, P2G<S>& P, S* affine, S* new_F) {
+  if constexpr (sizeof(S) == 4) {
+    p2g_particle_f32(m, C, F, P, affine, new_F);
+  } else {
+    // FP64: the reference's order of operations
+    S IC[9], Ftmp[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) IC[i] = m.dt * C[i] + ((i % 4 == 0) ? S(1) : S(0));
+    mm(IC, F, Ftmp);
+    svd3(Ftmp, P.U, P.s, P.V);
+    S eps[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      P.sm1[i] = P.s[i] - S(1);
+      P.sigc[i] = (S(0.05) < P.s[i]) ? P.s[i] : S(0.05);
+      eps[i] = mlog(P.sigc[i]);
+    }
+    S mean = fast_div(eps[0] + eps[1] + eps[2], S(3));
+#pragma unroll
+    for (int i = 0; i < 3; ++i) P.ehat[i] = eps[i] - mean;
+    P.nrm = msqrt(dot3(P.ehat, P.ehat) + S(1e-8));
+    P.dg = P.nrm - fast_div(m.ys, S(2) * m.mu);
+    P.yield = P.dg > S(0);
+    if (P.yield) {
+      P.k = fast_div(P.dg, P.nrm);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) P.e[i] = mexp(eps[i] - P.k * P.ehat[i]);
+      S UD[9];
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) UD[r * 3 + cc] = P.U[r * 3 + cc] * P.e[cc];
+      mmT(UD, P.V, P.newF);
+    } else {
+      P.k = S(0);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) P.e[i] = S(1);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) P.newF[i] = Ftmp[i];
+    }
+    P.J = det3(P.newF);
+    mmT(P.U, P.V, P.R);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) P.A[i] = P.newF[i] - P.R[i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) P.em1[i] = (P.yield ? P.e[i] : P.s[i]) - S(1);
+    p2g_affine(m, P, P.J - S(1), C, affine);
+    if (new_F) {
+#pragma unroll
+      for (int i = 0; i < 9; ++i) new_F[i] = P.newF[i];
+    }
+  }
+}
+// gradient of the singular values through the return map (yield branch of
+// compute_von_mises, mpm_simulator.py:166-180), from the diagonal of
+// M_N = U^T g_newF V (d loss / d e_i = M_N,ii)
+template <typename S>
+MPM_DI void return_map_sigma_grad(const P2G<S>& P, const S* MN, S* gs) {
+  S g_eps2[3], g_eps[3], g_ehat[3], g_k = S(0);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    g_eps2[i] = MN[i * 4] * P.e[i];
+    g_eps[i] = g_eps2[i];
+    g_k -= g_eps2[i] * P.ehat[i];
+    g_ehat[i] = -P.k * g_eps2[i];
+  }
+  S g_nrm = -fast_div(g_k * P.dg, P.nrm * P.nrm) + fast_div(g_k, P.nrm);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) g_ehat[i] += fast_div(g_nrm * P.ehat[i], P.nrm);
+  S sh = fast_div(g_ehat[0] + g_ehat[1] + g_ehat[2], S(3));
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    g_eps[i] += g_ehat[i] - sh;
+    gs[i] = (S(0.05) < P.s[i]) ? fast_div(g_eps[i], P.sigc[i]) : S(0);
+  }
+}
+
+// FP32 adjoint of p2g_particle_f32 in the SVD basis.  With G = U^T g_raw U
+// (g_raw = ks g_affine), e' = 1 + em1 the singular values of newF, and the
+// stress's matrices written in the bases U, V:
+//   U^T (g_raw newF) V   = G diag(e')        (the adjoint of A = newF - R)
+//   U^T (g_raw^T A) V    = G^T diag(e' - 1)  (through the right factor newF^T)
+//   U^T cof(newF) V      = J diag(1 / e')    (d det / d newF)
+// M_R = U^T g_R V = -2 mu G diag(e') and M_N = U^T g_newF V need no newF, A
+// or cofactor matrix.  The SVD part is svd3_bwd_factored_basis; the elastic
+// branch's direct newF = F_tmp term joins it in the same basis, so one
+// transform U Y V^T gives the gradient of F_tmp.
+MPM_DI void p2g_particle_vjp_f32(const MatConsts<float>& m, const float* C, const float* F, const P2G<float>& P,
+                                 const float* g_affine, const float* g_newF_in, float* g_C, float* g_F) {
+  float G[9], t9[9], MR[9], MN[9];
+  {
+    float g_raw[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) g_raw[i] = m.ks * g_affine[i];
+    mTm(P.U, g_raw, t9);
+    mm(t9, P.U, G);
+  }
+  const float g_J = m.lam * (2.f * P.J - 1.f) * (G[0] + G[4] + G[8]);  // tr g_raw = tr G
+  mTm(P.U, g_newF_in, t9);
+  mm(t9, P.V, MN);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const float ej = 1.f + P.em1[j];
+      const float a = 2.f * m.mu * G[i * 3 + j] * ej;
+      MR[i * 3 + j] = -a;
+      MN[i * 3 + j] += a + 2.f * m.mu * G[j * 3 + i] * P.em1[j] + (i == j ? fast_div(g_J * P.J, ej) : 0.f);
+    }
+  float gs[3] = {0.f, 0.f, 0.f}, Y[9];
+  if (P.yield) return_map_sigma_grad(P, MN, gs);
+  svd3_bwd_factored_basis(P.s, P.sm1, MR, MN, P.e, P.em1, 1.f - P.k, P.yield, gs, Y);
+  if (!P.yield) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Y[i] += MN[i];  // newF = F_tmp
+  }
+  float g_Ftmp[9];
+  mm(P.U, Y, t9);
+  mmT(t9, P.V, g_Ftmp);
+  mmT(g_Ftmp, F, t9);  // Ftmp = (I + dt C) F
+#pragma unroll
+  for (int i = 0; i < 9; ++i) g_C[i] = m.p_mass * g_affine[i] + m.dt * t9[i];
+  float IC[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) IC[i] = m.dt * C[i] + ((i % 4 == 0) ? 1.f : 0.f);
+  mTm(IC, g_Ftmp, g_F);
+}
+
+// FP64 adjoint of p2g_particle: the reference's order of operations, with
+// backward_svd as the reference writes it; g_C, g_F are written
+MPM_DI void p2g_particle_vjp_f64(const MatConsts<double>& m, const double* C, const double* F, const P2G<double>& P,
+                                 const double* g_affine, const double* g_newF_in, double* g_C, double* g_F) {
+  using S = double;
+  S g_raw[9], tmp[9], g_newF[9], g_R[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
     g_raw[i] = m.ks * g_affine[i];
     g_C[i] = m.p_mass * g_affine[i];
-    A[i] = P.newF[i] - P.R[i];
   }
   mm(g_raw, P.newF, tmp);  // d/dA of tr(g^T A newF^T)
 #pragma unroll
@@ -368,14 +572,15 @@ MPM_DI void p2g_particle_vjp(const MatConsts<S>& m, const S* C, const S* F, cons
     g_R[i] = S(-2) * m.mu * tmp[i];
     g_newF[i] = S(2) * m.mu * tmp[i] + g_newF_in[i];
   }
-  mTm(g_raw, A, tmp);  // d/dnewF of the right factor
+  mTm(g_raw, P.A, tmp);  // d/dnewF of the right factor
   S g_J = m.lam * (S(2) * P.J - S(1)) * (g_raw[0] + g_raw[4] + g_raw[8]);
   S cf[9];
   cof3(P.newF, cf);
 #pragma unroll
   for (int i = 0; i < 9; ++i) g_newF[i] += S(2) * m.mu * tmp[i] + g_J * cf[i];
-  S gU[9], gV[9], gs[3] = {S(0), S(0), S(0)}, g_Ftmp[9];
-  mm(g_R, P.V, gU);   // R = U V^T
+  S gs[3] = {S(0), S(0), S(0)}, g_Ftmp[9], gA[9];
+  S gU[9], gV[9];
+  mm(g_R, P.V, gU);  // R = U V^T
   mTm(g_R, P.U, gV);
   if (P.yield) {
     S GV[9], GtU[9], UtGV[9];
@@ -389,30 +594,13 @@ MPM_DI void p2g_particle_vjp(const MatConsts<S>& m, const S* C, const S* F, cons
         gV[r * 3 + cc] += GtU[r * 3 + cc] * P.e[cc];
       }
     mTm(P.U, GV, UtGV);
-    S g_eps2[3], g_eps[3], g_ehat[3], g_k = S(0);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      g_eps2[i] = UtGV[i * 4] * P.e[i];
-      g_eps[i] = g_eps2[i];
-      g_k -= g_eps2[i] * P.ehat[i];
-      g_ehat[i] = -P.k * g_eps2[i];
-    }
-    S g_nrm = -fast_div(g_k * P.dg, P.nrm * P.nrm) + fast_div(g_k, P.nrm);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) g_ehat[i] += fast_div(g_nrm * P.ehat[i], P.nrm);
-    S sh = fast_div(g_ehat[0] + g_ehat[1] + g_ehat[2], S(3));
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      g_eps[i] += g_ehat[i] - sh;
-      gs[i] = (S(0.05) < P.s[i]) ? fast_div(g_eps[i], P.sigc[i]) : S(0);
-    }
+    return_map_sigma_grad(P, UtGV, gs);
 #pragma unroll
     for (int i = 0; i < 9; ++i) g_Ftmp[i] = S(0);
   } else {
 #pragma unroll
     for (int i = 0; i < 9; ++i) g_Ftmp[i] = g_newF[i];
   }
-  S gA[9];
   svd3_bwd(P.U, P.s, P.V, gU, gs, gV, gA);
 #pragma unroll
   for (int i = 0; i < 9; ++i) g_Ftmp[i] += gA[i];
@@ -423,6 +611,14 @@ MPM_DI void p2g_particle_vjp(const MatConsts<S>& m, const S* C, const S* F, cons
 #pragma unroll
   for (int i = 0; i < 9; ++i) IC[i] = m.dt * C[i] + ((i % 4 == 0) ? S(1) : S(0));
   mTm(IC, g_Ftmp, g_F);
+}
+MPM_DI void p2g_particle_vjp(const MatConsts<float>& m, const float* C, const float* F, const P2G<float>& P,
+                             const float* g_affine, const float* g_newF_in, float* g_C, float* g_F) {
+  p2g_particle_vjp_f32(m, C, F, P, g_affine, g_newF_in, g_C, g_F);
+}
+MPM_DI void p2g_particle_vjp(const MatConsts<double>& m, const double* C, const double* F, const P2G<double>& P,
+                             const double* g_affine, const double* g_newF_in, double* g_C, double* g_F) {
+  p2g_particle_vjp_f64(m, C, F, P, g_affine, g_newF_in, g_C, g_F);
 }
 
 template <typename T, typename S>
@@ -507,10 +703,11 @@ MPM_DI void p2g_chunk(const Consts<T>& c, const T* __restrict__ st, T* __restric
     MatConsts<S> m = mat_consts<T, S>(c);
     P2G<S> P;
     S aff[9];
-    p2g_particle(m, C, F, P, aff);
+    S nF[9];
+    p2g_particle(m, C, F, P, aff, st_out ? nF : (S*)nullptr);
     if (st_out) {
 #pragma unroll
-      for (int k = 0; k < 9; ++k) st_out[(int64_t)(15 + k) * c.ld + p] = T(P.newF[k]);
+      for (int k = 0; k < 9; ++k) st_out[(int64_t)(15 + k) * c.ld + p] = T(nF[k]);
     }
     if (!ok) atomicOr(c.status, MPM_STATUS_OUT_OF_GRID);
     if (!finite(P.J)) atomicOr(c.status, MPM_STATUS_NONFINITE);
@@ -586,12 +783,13 @@ MPM_DI void p2g_chunk(const Consts<T>& c, const T* __restrict__ st, T* __restric
     }
   }
 }
-// FP32: 7 CTAs of 128 threads per SM (at most 73 registers, no spill);
-// measured 6 % faster than 6 CTAs
+// FP32: 7 CTAs of 128 threads per SM by default (at most 73 registers, no
+// spill; measured 6 % faster than 6 CTAs); MB > 0 compiles the kernel for MB
+// CTAs per SM instead (the autotuner's candidates, MpmTuning.p2g_ctas).
 // Strided: the CTAs stride over the particle chunks (the adjoint's recompute,
 // which exits at once when the grid store holds the substep)
-template <typename T, typename S, bool Strided = false>
-__global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 7 : 4) k_p2g(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
+template <typename T, typename S, bool Strided = false, int MB = 0>
+__global__ void __launch_bounds__(128, MB > 0 ? MB : ((sizeof(T) == 4 && sizeof(S) == 4) ? 7 : 4)) k_p2g(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
                                              const int* __restrict__ pscene, Node<T>* __restrict__ grid,
                                              const int64_t* __restrict__ saved) {
   if (saved && *saved >= 0) return;  // the grid of this substep was restored from the grid store
@@ -854,10 +1052,11 @@ __global__ void __launch_bounds__(128) k_g2p(Consts<T> c, const T* __restrict__ 
 // g2p.grad: writes the x rows of g0 (partial) and scatters into g_grid
 // st1 (frame f+1, may be null): its v rows are the g2p output, so the clamp
 // mask needs no second gather of the grid.
-// FP32: 6 CTAs of 128 threads per SM (at most 80 registers, a small spill);
-// measured 20 % faster than the unconstrained 108 registers
-template <typename T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 6 : 2) k_g2p_adj(Consts<T> c, const T* __restrict__ st, const T* __restrict__ st1,
+// FP32: 6 CTAs of 128 threads per SM by default (at most 80 registers, a
+// small spill; measured 20 % faster than the unconstrained 108 registers);
+// MB > 0: MB CTAs per SM (MpmTuning.g2p_adj_ctas)
+template <typename T, int MB = 0>
+__global__ void __launch_bounds__(128, MB > 0 ? MB : (sizeof(T) == 4 ? 6 : 2)) k_g2p_adj(Consts<T> c, const T* __restrict__ st, const T* __restrict__ st1,
                                                  const T* __restrict__ g1, T* __restrict__ g0,
                                                  const int* __restrict__ pscene, const Node<T>* __restrict__ grid,
                                                  Node<T>* __restrict__ g_grid) {
@@ -1138,10 +1337,11 @@ __global__ void __launch_bounds__(64) k_grid_op_adj(Consts<T> c, const int* __re
 
 // p2g.grad + svd_grad + compute_F_tmp.grad: gathers g_in; reads the partial
 // x gradient left in g0 by k_g2p_adj and writes all 24 rows of g0.
-// FP32: at most 102 registers (5 CTAs of 128 threads per SM; a small spill),
-// measured 3 % faster than 4 CTAs at 128 registers
-template <typename T, typename S>
-__global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 5 : 2) k_p2g_adj(Consts<T> c, const T* __restrict__ st, const T* __restrict__ g1,
+// FP32: at most 102 registers by default (5 CTAs of 128 threads per SM; a
+// small spill), measured 3 % faster than 4 CTAs at 128 registers; MB > 0: MB
+// CTAs per SM (MpmTuning.p2g_adj_ctas)
+template <typename T, typename S, int MB = 0>
+__global__ void __launch_bounds__(128, MB > 0 ? MB : ((sizeof(T) == 4 && sizeof(S) == 4) ? 5 : 2)) k_p2g_adj(Consts<T> c, const T* __restrict__ st, const T* __restrict__ g1,
                                                  T* __restrict__ g0, const int* __restrict__ pscene,
                                                  const Node<T>* __restrict__ g_in) {
   int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1167,7 +1367,7 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && sizeof(S) == 4) ? 5 : 
   MatConsts<S> m = mat_consts<T, S>(c);
   P2G<S> P;
   S aff[9];
-  p2g_particle(m, C, F, P, aff);
+  p2g_particle(m, C, F, P, aff, (S*)nullptr);
   T affine[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) affine[k] = T(aff[k]);

@@ -17,14 +17,32 @@ namespace mpm {
 
 MPM_DI float msqrt(float x) { return sqrtf(x); }
 MPM_DI double msqrt(double x) { return sqrt(x); }
-// FP32 exp and log by the hardware approximations (__expf, __logf): they
-// serve the return map's log/exp of singular values near 1 and the contact
-// softness exp(-dist * softness), where their error stays below the FP32
-// substep's own rounding noise
-MPM_DI float mexp(float x) { return __expf(x); }
+// exp and log of the return map (log of singular values near 1, exp of the
+// projected strains): the accurate library functions.  __logf's error near 1
+// is absolute (about 2^-21), i.e. hundreds of ulp of a strain of 1e-3.
+MPM_DI float mexp(float x) { return expf(x); }
 MPM_DI double mexp(double x) { return exp(x); }
-MPM_DI float mlog(float x) { return __logf(x); }
+MPM_DI float mlog(float x) { return logf(x); }
 MPM_DI double mlog(double x) { return log(x); }
+// log(1 + x) and exp(x) - 1 for the FP32 strains (x = s - 1 of a singular
+// value, or a projected log-strain), accurate to the result's own precision:
+// for |x| < 1/64 by their Taylor series (truncation below 3e-12 and 2e-13
+// relative), otherwise by the library's log1pf / expm1f.
+MPM_DI float log1p_strain(float x) {
+  if (fabsf(x) < 0.015625f)
+    return x * fmaf(x, fmaf(x, fmaf(x, fmaf(x, fmaf(x, -1.f / 6.f, 0.2f), -0.25f), 1.f / 3.f), -0.5f), 1.f);
+  return log1pf(x);
+}
+MPM_DI float expm1_strain(float x) {
+  if (fabsf(x) < 0.015625f)
+    return x * fmaf(x, fmaf(x, fmaf(x, fmaf(x, fmaf(x, 1.f / 720.f, 1.f / 120.f), 1.f / 24.f), 1.f / 6.f), 0.5f), 1.f);
+  return expm1f(x);
+}
+// exp of the contact softness exp(-dist * softness) (primive_base.py:99), FP32
+// by the hardware approximation: its relative error (a few ulp over the
+// influence range exp(x) > 0.1) stays below the substep's rounding noise
+MPM_DI float mexp_fast(float x) { return __expf(x); }
+MPM_DI double mexp_fast(double x) { return exp(x); }
 MPM_DI float msin(float x) { return sinf(x); }
 MPM_DI double msin(double x) { return sin(x); }
 MPM_DI float mcos(float x) { return cosf(x); }

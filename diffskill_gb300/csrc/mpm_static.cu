@@ -13,12 +13,16 @@
 //
 // The scratch is the file-scope array g_static_scratch below (20 MiB + 64 KiB).  Every GPU that
 // loads this library holds it until the process exits.  All calls share it
-// and it keeps the last call's contents: the status word, the active-block
-// flags and the grid blocks the scatter accumulates into are cleared on every
-// call; the scene-index region is zeroed once per device and never written
-// afterwards.  Calls whose
+// and it keeps the last call's contents: the tool table, the scratch status
+// word, the active-block flags and the grid blocks the scatter accumulates
+// into are rewritten or cleared on every call; the scene-index region is
+// zeroed once per device and never written afterwards.  Calls whose
 // kernels overlap on the GPU (different streams, or different host threads,
 // on the same device) race on the array; serialise them.
+//
+// Per call the host issues kernel launches only: the scene's tool table
+// travels by value as a kernel parameter (k_static_setup), so no pageable
+// host-to-device copy orders the call against the host.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -32,7 +36,7 @@
 namespace {
 
 // Layout of the scratch array:
-//   [0, 4)                      status word
+//   [0, 4)                      status word (when the caller passes none)
 //   [16, 24)                    tool offsets {0, n_tools} of the one scene
 //   [256, 256 + 8*tool size)    tool table
 //   [4096, 4096 + 16 + 8000)    active-block counter and flags (<= 20^3 blocks)
@@ -94,13 +98,39 @@ int scratch_base(int dev, unsigned char** out) {
 
 bool aligned16(const void* p) { return p && (reinterpret_cast<uintptr_t>(p) % 16 == 0); }
 
+// The per-call set-up, passed by value (about 2.1 KB of kernel parameters).
+struct StaticSetup {
+  int32_t n_tools;
+  int32_t clear_status;  // zero the scratch status word (the caller gave none)
+  MpmToolDesc tools[mpm::MAX_TOOLS_PER_SCENE];
+};
+
+// One warp: the tool offsets {0, n_tools}, the descriptor table, the tools in
+// the compute precision T, and the scratch status word.
+template <typename T>
+__global__ void __launch_bounds__(32) k_static_setup(StaticSetup a) {
+  unsigned char* base = g_static_scratch;
+  const int i = threadIdx.x;
+  if (i == 0) {
+    int* toff = reinterpret_cast<int*>(base + 16);
+    toff[0] = 0;
+    toff[1] = a.n_tools;
+    if (a.clear_status) *reinterpret_cast<unsigned int*>(base) = 0u;
+  }
+  if (i < a.n_tools) {
+    reinterpret_cast<MpmToolDesc*>(base + 256)[i] = a.tools[i];
+    mpm::to_tool(a.tools[i], reinterpret_cast<mpm::Tool<T>*>(base + kToolsT)[i]);
+  }
+}
+
 }  // namespace
 
 extern "C" {
 
 // No counterpart in the reference.  See include/mpm_gb300.h.
 int mpm_substep_fwd_static(const MpmParams* params, const MpmToolDesc* tools, int32_t n_tools, const void* state_f,
-                           void* state_f1, const double* pose_f, const double* pose_f1, void* stream) {
+                           void* state_f1, const double* pose_f, const double* pose_f1, uint32_t* status,
+                           void* stream) {
   if (!params) return set_err(MPM_E_INVALID, "mpm_substep_fwd_static: params is NULL");
   const MpmParams& p = *params;
   if (p.abi_version != MPM_ABI_VERSION) return set_err(MPM_E_INVALID, "mpm_substep_fwd_static: ABI version mismatch");
@@ -134,6 +164,8 @@ int mpm_substep_fwd_static(const MpmParams* params, const MpmToolDesc* tools, in
                                   "device pointers");
   if (n_tools > 0 && (!aligned16(pose_f) || !aligned16(pose_f1)))
     return set_err(MPM_E_INVALID, "mpm_substep_fwd_static: pose_f and pose_f1 must be 16-byte aligned");
+  if (status && reinterpret_cast<uintptr_t>(status) % 4 != 0)
+    return set_err(MPM_E_INVALID, "mpm_substep_fwd_static: status must be a 4-byte aligned device pointer");
 
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -143,13 +175,16 @@ int mpm_substep_fwd_static(const MpmParams* params, const MpmToolDesc* tools, in
   if (rc != MPM_OK) return rc;
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int toff[2] = {0, n_tools};
-  e = cudaMemsetAsync(base, 0, 4, s);  // status word
-  if (e == cudaSuccess) e = cudaMemcpyAsync(base + 16, toff, sizeof(toff), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess && n_tools > 0)
-    e = cudaMemcpyAsync(base + 256, tools, size_t(n_tools) * sizeof(MpmToolDesc), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess)
-    e = mpm::convert_tools(p.precision, n_tools, reinterpret_cast<const MpmToolDesc*>(base + 256), base + kToolsT, s);
+  StaticSetup su;
+  std::memset(&su, 0, sizeof(su));
+  su.n_tools = n_tools;
+  su.clear_status = status ? 0 : 1;
+  for (int i = 0; i < n_tools; ++i) su.tools[i] = tools[i];
+  if (p.precision == MPM_PREC_FP64)
+    k_static_setup<double><<<1, 32, 0, s>>>(su);
+  else
+    k_static_setup<float><<<1, 32, 0, s>>>(su);
+  e = cudaGetLastError();
   if (e != cudaSuccess) return set_err(MPM_E_CUDA, std::string("mpm_substep_fwd_static: ") + cudaGetErrorString(e));
 
   int64_t launches = 0;
@@ -160,7 +195,9 @@ int mpm_substep_fwd_static(const MpmParams* params, const MpmToolDesc* tools, in
   L.tools = reinterpret_cast<const MpmToolDesc*>(base + 256);
   L.tool_off = reinterpret_cast<const int*>(base + 16);
   L.n_tools = n_tools;
-  L.status = reinterpret_cast<unsigned int*>(base);
+  // the caller's status word when given (sticky: the caller clears it), else
+  // the scratch word, which is cleared per call and not reported
+  L.status = status ? reinterpret_cast<unsigned int*>(status) : reinterpret_cast<unsigned int*>(base);
   L.grid_a = base + kHeader + kScene;              // active blocks cleared by the launcher before the scatter
   L.grid_b = base + kHeader + kScene + grid_bytes;  // fully written by grid_op
   L.grid_c = nullptr;

@@ -648,7 +648,7 @@ template <typename T>
 MPM_DI bool collide_fwd(const Tool<T>& t, const T* pos0, const T* rot0, T gap0, const T* pos1, const T* rot1,
                         const T* p, T dt, const T* vin, T* vout) {
   T dist = shape_sdf(t, pos0, rot0, gap0, p);
-  T e = mexp(-dist * t.softness);
+  T e = mexp_fast(-dist * t.softness);
   T infl = (e < T(1)) ? e : T(1);
 #pragma unroll
   for (int k = 0; k < 3; ++k) vout[k] = vin[k];
@@ -679,7 +679,7 @@ MPM_DI void collide_vjp(const Tool<T>& t, const T* pos0, const T* rot0, T gap0, 
                         const T* p, T dt, const T* vin, const T* gout, T* gvin, T* gpos0, T* grot0, T* ggap0,
                         T* gpos1, T* grot1) {
   T dist = shape_sdf(t, pos0, rot0, gap0, p);
-  T e = mexp(-dist * t.softness);
+  T e = mexp_fast(-dist * t.softness);
   T infl = (e < T(1)) ? e : T(1);
   if (!((t.softness > T(0) && infl > T(0.1)) || dist <= T(0))) {
 #pragma unroll

@@ -480,18 +480,26 @@ class Horizon:
             worst = n_slots * eng.S * (eng.n_grid // 4) ** 3
             self.store = GridStore(eng, n_slots, min(worst, store_budget_bytes // block_bytes))
         # periodic re-sorting of the particles by cell
-        if resort_every is None:
-            resort_every = k * (-(-eng.n_sub // k))
-        R = int(resort_every)
-        if R and R % k != 0:
-            raise ValueError(f"resort_every ({R}) must be a multiple of the checkpoint interval ({k})")
-        self.R = R if 0 < R < self.F else 0
-        self.boundaries = list(range(self.R, self.F, self.R)) if self.R else []
-        self.perms = torch.zeros((max(len(self.boundaries), 1), max(eng.P, 1)), dtype=torch.int64, device=dev)
+        self.perms = None
+        self.set_resort_every(k * (-(-eng.n_sub // k)) if resort_every is None else resort_every)
         counts = torch.as_tensor(np.diff(eng.offsets), device=dev)
         self.pscene = torch.repeat_interleave(torch.arange(eng.S, device=dev), counts)
         self.pscene32 = self.pscene.to(torch.int32)
         self._tmp = torch.empty((N_ROWS, max(eng.P, 1)), dtype=dt, device=dev)
+
+    def set_resort_every(self, resort_every: int) -> None:
+        """Re-sort the particles by cell every ``resort_every`` substeps (a
+        multiple of the checkpoint interval; 0 = never).  Takes effect from
+        the next ``forward``; do not change it between a forward and its
+        backward, nor after a CUDA graph captured them."""
+        R = int(resort_every)
+        if R < 0 or (R and R % self.k != 0):
+            raise ValueError(f"resort_every ({R}) must be 0 or a multiple of the checkpoint interval ({self.k})")
+        self.R = R if 0 < R < self.F else 0
+        self.boundaries = list(range(self.R, self.F, self.R)) if self.R else []
+        need = (max(len(self.boundaries), 1), max(self.eng.P, 1))
+        if self.perms is None or self.perms.shape[0] < need[0]:
+            self.perms = torch.zeros(need, dtype=torch.int64, device=self.eng.device)
 
     def bytes(self) -> int:
         return sum(t.numel() * t.element_size() for t in
@@ -502,8 +510,15 @@ class Horizon:
     def final(self) -> torch.Tensor:
         return self.ckpt[self.n_ckpt - 1]
 
-    def _sort_frame(self, frame: torch.Tensor, b: int) -> None:
-        """Sort the particles of ``frame`` by (scene, 4^3 block, cell) in place; keep the permutation."""
+    def sort_frame(self, frame: torch.Tensor) -> None:
+        """Sort the particles of ``frame`` by (scene, 4^3 block, cell) in place, on
+        the device (an initial state: losses and action gradients do not depend
+        on the particle order)."""
+        self._sort_frame(frame, None)
+
+    def _sort_frame(self, frame: torch.Tensor, b: Optional[int]) -> None:
+        """Sort the particles of ``frame`` by (scene, 4^3 block, cell) in place;
+        keep the permutation as boundary ``b``'s (unless ``b`` is None)."""
         eng, P = self.eng, self.eng.P
         if P == 0:
             return
@@ -516,7 +531,8 @@ class Horizon:
         loc = ((base[0] & 3) << 4) | ((base[1] & 3) << 2) | (base[2] & 3)
         key = ((self.pscene32 if it == torch.int32 else self.pscene) * (nb ** 3) + blk) * 64 + loc
         perm = torch.argsort(key)
-        self.perms[b].copy_(perm)
+        if b is not None:
+            self.perms[b].copy_(perm)
         torch.index_select(frame[:, :P], 1, perm, out=self._tmp)
         frame[:, :P].copy_(self._tmp)
 
@@ -528,8 +544,11 @@ class Horizon:
         self._tmp.copy_(g[:, :P])
         g[:, :P].index_copy_(1, self.perms[b], self._tmp)
 
-    def forward(self, state0: torch.Tensor, actions: torch.Tensor, pose0: Optional[torch.Tensor] = None) -> None:
-        """Run all actions: ``GradModel.forward_step`` for each action (function.py:166-175)."""
+    def forward(self, state0: torch.Tensor, actions: torch.Tensor, pose0: Optional[torch.Tensor] = None,
+                keep_grids: bool = True) -> None:
+        """Run all actions: ``GradModel.forward_step`` for each action (function.py:166-175).
+
+        ``keep_grids=False`` skips the grid store (a forward that no adjoint follows)."""
         eng, n = self.eng, self.eng.n_sub
         main = torch.cuda.current_stream()
         self.ckpt[0].copy_(state0)
@@ -547,7 +566,7 @@ class Horizon:
                     ev = torch.cuda.Event()
                     ev.record(self.side)
                     ready.append(ev)
-        store = self.store if (self.store is not None and self.k == 1) else None
+        store = self.store if (keep_grids and self.store is not None and self.k == 1) else None
         if store is not None:
             store.reset()
         cur = self.ckpt[0]

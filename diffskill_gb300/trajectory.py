@@ -30,6 +30,27 @@ def spatial_order(x: np.ndarray, n_grid: int) -> np.ndarray:
     return np.argsort(blk * 64 + loc, kind="stable")
 
 
+def adam_update(actions: torch.Tensor, grad: torch.Tensor, mask: torch.Tensor, m: torch.Tensor, v: torch.Tensor,
+                t: torch.Tensor, betas=(0.9, 0.999), lr: float = 0.01, eps: float = 1e-8) -> None:
+    """One ``torch.optim.Adam`` step on ``actions`` (no weight decay, no
+    amsgrad: ``actions -= lr * m_hat / (sqrt(v_hat) + eps)``), then
+    ``clamp(-1, 1)`` and the action mask, as ``Solver.solve_one_plan`` applies
+    them (plb/optimizer/solver.py:98, 128-133).  The step count ``t`` is a
+    device tensor, so the bias corrections change between replays of a CUDA
+    graph that captured this update.  ``mask`` zeroes the padding lanes of the
+    [A, T, 8] action layout (their gradient is zero too)."""
+    b1, b2 = float(betas[0]), float(betas[1])
+    g = grad * mask
+    t.add_(1)
+    m.mul_(b1).add_(g, alpha=1 - b1)
+    v.mul_(b2).addcmul_(g, g, value=1 - b2)
+    bc1 = 1 - torch.pow(b1, t)
+    bc2 = 1 - torch.pow(b2, t)
+    denom = (v / bc2).sqrt_().add_(eps)
+    actions.sub_(lr * (m / bc1) / denom)
+    actions.clamp_(-1, 1).mul_(mask)
+
+
 def _check_compatible(scenes: Sequence[Scene]) -> None:
     s0 = scenes[0].sim
     for sc in scenes[1:]:
@@ -44,7 +65,8 @@ def _check_compatible(scenes: Sequence[Scene]) -> None:
 
 class BatchedTrajectory:
     def __init__(self, scenes: Sequence[Scene], ckpt_every: Union[int, str, None] = None, lr: float = 0.01,
-                 betas=(0.9, 0.999), eps: float = 1e-8, softness: float = 666.0, sort_particles: bool = True):
+                 betas=(0.9, 0.999), eps: float = 1e-8, softness: float = 666.0, sort_particles: bool = True,
+                 autotune: bool = False):
         scenes = list(scenes)
         _check_compatible(scenes)
         self.scenes = scenes
@@ -69,10 +91,21 @@ class BatchedTrajectory:
         self.m = torch.zeros_like(self.actions)
         self.v = torch.zeros_like(self.actions)
         self.t = torch.zeros((), dtype=torch.float64, device=eng.device)
-        self._b = torch.tensor(list(betas), dtype=torch.float64, device=eng.device)
         self.loss = torch.zeros(eng.S, dtype=torch.float64, device=eng.device)
         self.grad = torch.zeros_like(self.actions)
         self.graph: Optional[torch.cuda.CUDAGraph] = None
+        self.tuning = None
+        if autotune:
+            self.autotune()
+
+    def autotune(self, **kw):
+        """Pick launch shapes and the re-sort cadence for this batch by
+        measurement (``diffskill_gb300.autotune.tune``); before ``capture``."""
+        from .autotune import tune
+        if self.graph is not None:
+            raise RuntimeError("autotune before capturing the CUDA graph")
+        self.tuning = tune(self, **kw)
+        return self.tuning
 
     @property
     def particle_substeps(self) -> int:
@@ -84,18 +117,30 @@ class BatchedTrajectory:
         self.loss.copy_(hz.loss(self.targets, self.density_weight, self.contact_weight))
         self.grad.copy_(hz.backward())
 
+    def set_initial_positions(self, x: torch.Tensor) -> None:
+        """New initial positions ``x`` ([3, P] on the device, scenes concatenated
+        in their order, particles of a scene in any order): the initial state
+        becomes ``reset_kernel``'s (mpm_simulator.py:402-409: v = 0, C = 0,
+        F = I) at ``x``, with each scene's particles sorted by grid cell on the
+        device."""
+        P = self.eng.P
+        st = self.state0
+        st[0:3, :P].copy_(x)
+        st[3:24, :P].zero_()
+        st[15, :P].fill_(1)
+        st[19, :P].fill_(1)
+        st[23, :P].fill_(1)
+        self.hz.sort_frame(st)
+
+    def forward_only(self) -> None:
+        """Forward of every action and the per-scene loss, no adjoint."""
+        hz = self.hz
+        hz.forward(self.state0, self.actions, keep_grids=False)
+        self.loss.copy_(hz.loss(self.targets, self.density_weight, self.contact_weight, need_grad=False))
+
     def adam(self) -> None:
         """torch.optim.Adam update, then clamp to [-1, 1] and mask (solver.py:128-133)."""
-        b1, b2 = self.betas
-        g = self.grad * self.mask
-        self.t.add_(1)
-        self.m.mul_(b1).add_(g, alpha=1 - b1)
-        self.v.mul_(b2).addcmul_(g, g, value=1 - b2)
-        bc1 = 1 - torch.pow(self._b[0], self.t)
-        bc2 = 1 - torch.pow(self._b[1], self.t)
-        denom = (self.v / bc2).sqrt_().add_(self.eps)
-        self.actions.sub_(self.lr * (self.m / bc1) / denom)
-        self.actions.clamp_(-1, 1).mul_(self.mask)
+        adam_update(self.actions, self.grad, self.mask, self.m, self.v, self.t, self.betas, self.lr, self.eps)
 
     def step(self) -> None:
         """One optimisation iteration (replays the CUDA graph when captured)."""
@@ -107,18 +152,26 @@ class BatchedTrajectory:
 
     def capture(self) -> None:
         """Capture forward + backward + Adam of one iteration as a CUDA graph."""
+        self.graph = self._capture(lambda: (self.forward_backward(), self.adam()), self.forward_backward)
+
+    def capture_forward(self) -> torch.cuda.CUDAGraph:
+        """Capture the forward and the loss of one iteration (no adjoint) as a
+        CUDA graph, returned for the caller to replay."""
+        return self._capture(self.forward_only, self.forward_only)
+
+    @staticmethod
+    def _capture(body, warm) -> torch.cuda.CUDAGraph:
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(s):  # warm allocations outside the capture
-            self.forward_backward()
+            warm()
         torch.cuda.current_stream().wait_stream(s)
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
-            self.forward_backward()
-            self.adam()
+            body()
         torch.cuda.synchronize()
-        self.graph = g
+        return g
 
     def reset_optimizer(self, actions: Optional[List] = None) -> None:
         if actions is not None:

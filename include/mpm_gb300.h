@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define MPM_ABI_VERSION 3
+#define MPM_ABI_VERSION 4
 
 /* return codes */
 #define MPM_OK 0
@@ -121,6 +121,19 @@ typedef struct MpmGridStore {
   int32_t reserved;
 } MpmGridStore;
 
+/* Launch shapes of the substep kernels (no counterpart in the reference,
+ * whose launch shapes are Taichi's).  A field of 0 keeps the default.  The
+ * FP32 particle kernels are compiled for several CTAs-per-SM targets (each a
+ * register budget: 65536 / (128 * CTAs) registers per thread); the grid
+ * kernels stride over the active blocks with grid_ctas_per_sm * SMs CTAs.
+ * diffskill_gb300/autotune.py times the candidates and picks per workload. */
+typedef struct MpmTuning {
+  int32_t p2g_ctas;          /* FP32 p2g: 6, 7 (default) or 8 CTAs of 128 threads per SM */
+  int32_t g2p_adj_ctas;      /* FP32 g2p.grad: 5, 6 (default), 7 or 8 */
+  int32_t p2g_adj_ctas;      /* FP32 p2g.grad: 4, 5 (default) or 6 */
+  int32_t grid_ctas_per_sm;  /* grid_op / grid_op.grad: 2 .. 64 (default 16) */
+} MpmTuning;
+
 typedef struct MpmHandle MpmHandle;
 
 const char* mpm_version(void);
@@ -195,6 +208,13 @@ int mpm_substep_bwd(MpmHandle* h, const void* state_f, const void* state_f1, con
  * columns (the re-sort), which leaves the set of blocks unchanged.  Any
  * adjoint substep ends the chain.  No counterpart in the reference. */
 int mpm_set_chained(MpmHandle* h, int32_t on);
+
+/* Sets the launch shapes of the handle's later substeps (MpmTuning; a value
+ * outside a field's candidates returns MPM_E_INVALID and changes nothing).
+ * No counterpart in the reference. */
+int mpm_set_tuning(MpmHandle* h, const MpmTuning* tuning);
+/* Reads the handle's launch shapes, defaults filled in. */
+int mpm_get_tuning(MpmHandle* h, MpmTuning* tuning);
 
 /* mpm_substep_fwd that also keeps the substep's forward grids in store slot
  * `slot` (no counterpart in the reference, whose substep_grad always
@@ -341,19 +361,25 @@ int mpm_render_trace(MpmHandle* h, const MpmRenderVolume* vol, const MpmRenderVi
  * or latency-bound loops that cannot afford the device-wide synchronisation
  * of cudaMalloc/cudaFree.  No handle: params (n_scenes = 1) and the host tool
  * table are passed per call; the caller still owns state_f, state_f1, pose_f
- * and pose_f1.  Grid scratch, tool table and status word live in one
- * file-scope static device array of 20 MiB + 64 KiB, held by every GPU that
- * loads the library until the process exits.  Limits: n_particles <= 2^20;
- * two grids of n_grid^3 nodes within 16 MiB (n_grid <= 80 in FP32, <= 64 in
- * FP64); at most 8 tools.  Larger sizes return MPM_E_INVALID; the message is
- * read with mpm_last_error(NULL, ...).  The first call on a device performs
- * set-up (cudaGetSymbolAddress on that device and zeroing of the array's
- * scene-index region); make that first call before any stream capture.  All
- * calls share the array: calls whose kernels overlap on the GPU race, so
- * serialise them.  The device status word is cleared per call and not
- * reported. */
+ * and pose_f1.  Grid scratch and tool table live in one file-scope static
+ * device array of 20 MiB + 64 KiB, held by every GPU that loads the library
+ * until the process exits.  Limits: n_particles <= 2^20; two grids of
+ * n_grid^3 nodes within 16 MiB (n_grid <= 80 in FP32, <= 64 in FP64); at most
+ * 8 tools, of types MPM_TOOL_SPHERE .. MPM_TOOL_GRIPPER (0-4) only.  Larger
+ * sizes or other tool types return MPM_E_INVALID; the message is read with
+ * mpm_last_error(NULL, ...).  The tool table is passed to the device by value
+ * as a kernel parameter: a call issues kernel launches only, no host-to-device
+ * copy.  status (may be NULL): a caller-owned 4-byte aligned device word into
+ * which the call's kernels OR the MPM_STATUS_* bits (a particle stencil
+ * outside the grid, skipped; a NaN/Inf); it is sticky, the caller clears and
+ * reads it.  With NULL the bits go to a scratch word and are not reported.
+ * The first call on a device performs set-up (cudaGetSymbolAddress on that
+ * device and zeroing of the array's scene-index region); make that first call
+ * before any stream capture.  All calls share the array: calls whose kernels
+ * overlap on the GPU race, so serialise them. */
 int mpm_substep_fwd_static(const MpmParams* params, const MpmToolDesc* tools, int32_t n_tools, const void* state_f,
-                           void* state_f1, const double* pose_f, const double* pose_f1, void* stream);
+                           void* state_f1, const double* pose_f, const double* pose_f1, uint32_t* status,
+                           void* stream);
 
 /* Reads the sticky device status word (synchronises the stream). */
 int mpm_status(MpmHandle* h, uint32_t* status, int32_t clear, void* stream);

@@ -7,7 +7,8 @@ central moments in world units (node I at I*dx), and the support box.  The
 quadratic B-spline stencil reproduces linear functions exactly and adds a
 variance of dx^2/4 per axis, so these statistics pin p_mass, the grid layout
 and the weights of the oracle's compute_grid_m without the (unshipped)
-particle sets.  Run in the build container: python tests/golden/make_golden.py
+particle sets.  Usage: python tests/golden/make_golden.py REFERENCE_CHECKOUT
+(the root of a DiffSkill checkout, the directory holding plb/).
 """
 import glob
 import json
@@ -16,7 +17,6 @@ import sys
 
 import numpy as np
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "density_assets.json")
 
 
@@ -35,7 +35,12 @@ def stats(a: np.ndarray) -> dict:
 
 
 def main() -> None:
-    files = sorted(glob.glob(os.path.join(REF, "plb/envs/assets/*3D-v*.npy")))
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py REFERENCE_CHECKOUT  (the directory holding plb/envs/assets)")
+    ref = sys.argv[1]
+    files = sorted(glob.glob(os.path.join(ref, "plb/envs/assets/*3D-v*.npy")))
+    if not files:
+        sys.exit(f"no plb/envs/assets/*3D-v*.npy under {ref}")
     out = {"source": "plb/envs/assets/*3D-v*.npy", "grids": {}}
     for f in files:
         out["grids"][os.path.basename(f)] = stats(np.load(f))
