@@ -1,9 +1,10 @@
 """GPU (sm_103a) parity against the FP64 CPU oracle, through the C ABI.
 
 Tolerances (stated per test): the FP64 GPU path must match the oracle to
-near round-off (1e-9 relative per row group); FP32 paths are checked at the
-looser bounds that single precision allows (forward 1e-4 relative to the
-row-group magnitude, gradients 1e-3 / 5e-2 as stated below).
+near round-off (1e-9 relative per row group); FP32 paths to what single
+precision allows: one substep 1e-4 (forward) and 2e-4 (adjoint) relative to
+the row-group magnitude, trajectory action gradients 1e-3 (the bound the
+benchmark's accuracy claim states), positions after one action 1e-4.
 """
 import numpy as np
 import pytest
@@ -55,7 +56,7 @@ def test_substep_forward_matches_oracle(gpu_lib, prec):
     del act
 
 
-@pytest.mark.parametrize("prec,tol", [("fp64", 1e-8), ("fp32_svd64", 2e-3), ("fp32", 2e-3)])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-8), ("fp32_svd64", 2e-4), ("fp32", 2e-4)])
 def test_substep_adjoint_matches_oracle(gpu_lib, prec, tol):
     tools = all_tools()
     sc = small_scene(n=3000, tools=tools, precision=prec)
@@ -130,8 +131,8 @@ def _traj(eng, sc, k):
     return float(loss.sum()), eng.collapse_action_grad(g)[0].cpu().numpy(), hz
 
 
-@pytest.mark.parametrize("prec,loss_tol,grad_tol", [("fp64", 1e-9, 1e-6), ("fp32_svd64", 1e-3, 5e-2),
-                                                    ("fp32", 1e-3, 5e-2)])
+@pytest.mark.parametrize("prec,loss_tol,grad_tol", [("fp64", 1e-9, 1e-6), ("fp32_svd64", 1e-5, 1e-3),
+                                                    ("fp32", 1e-5, 1e-3)])
 def test_trajectory_loss_and_action_grad(gpu_lib, prec, loss_tol, grad_tol):
     """Config-1 shape (capsule, density L1 to the +0.1-shifted dough), 2 actions x 50 substeps."""
     sc = small_scene(n=4000, n_actions=2, substeps=50, precision=prec)
@@ -142,6 +143,26 @@ def test_trajectory_loss_and_action_grad(gpu_lib, prec, loss_tol, grad_tol):
     assert eng.status() == 0
     assert abs(loss - ref_loss) / abs(ref_loss) < loss_tol, (loss, ref_loss)
     assert rel_err(grad, ref_grad) < grad_tol, (grad, ref_grad)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp32_svd64"])
+def test_positions_after_one_action_match_oracle(gpu_lib, prec):
+    """The FP32 state after one action (50 substeps) of config 1 (10k particles
+    in a 0.2 x 0.1 x 0.2 box, capsule): every particle position within 1e-4
+    relative (to the largest coordinate) of the FP64 oracle's."""
+    from diffskill_gb300 import scenes
+    sc = scenes.config1(n_actions=1, dt=1e-4)
+    sc.sim.precision = prec
+    ro = Oracle(sc.sim, sc.tools).rollout(sc.x0, sc.actions, keep_frames=False)
+    eng = make_engine(sc)
+    hz = Horizon(eng, 1, ckpt_every=50)
+    hz.forward(eng.init_state([sc.x0]), eng.expand_actions([sc.actions]))
+    torch.cuda.synchronize()
+    assert eng.status() == 0
+    x = hz.final[0:3, :eng.P].double().cpu().numpy().T
+    xr = ro["final"][:, 0:3]
+    assert np.abs(xr - sc.x0).max() > 1e-3  # the dough moved
+    assert rel_err(x, xr) < 1e-4, rel_err(x, xr)
 
 
 def test_checkpoint_recompute_equals_store_all(gpu_lib):
@@ -289,7 +310,7 @@ def test_invalid_arguments_raise(gpu_lib):
         MpmEngine(bad_sim, [[bad]], [10])
 
 
-@pytest.mark.parametrize("prec,loss_tol,grad_tol", [("fp64", 1e-9, 1e-6), ("fp32", 1e-3, 5e-2)])
+@pytest.mark.parametrize("prec,loss_tol,grad_tol", [("fp64", 1e-9, 1e-6), ("fp32", 1e-5, 1e-3)])
 def test_sorted_particles_warp_aggregated_scatter_matches_oracle(gpu_lib, prec, loss_tol, grad_tol):
     """BatchedTrajectory sorts particles by cell, so the p2g and g2p.grad scatters
     take the warp-segmented reduction path; results must still match the oracle."""
@@ -363,7 +384,7 @@ def test_resorting_particles_keeps_loss_and_gradients(gpu_lib, k):
 # RollingPin(Ext), Chopsticks, Cylinder, Torus, Gripper2 and the tool-tool
 # collision projection
 # ----------------------------------------------------------------------------
-@pytest.mark.parametrize("prec,fwd_tol,bwd_tol", [("fp64", 1e-9, 1e-8), ("fp32", 1e-4, 2e-3)])
+@pytest.mark.parametrize("prec,fwd_tol,bwd_tol", [("fp64", 1e-9, 1e-8), ("fp32", 1e-4, 1e-3)])
 def test_more_tools_substep_matches_oracle(gpu_lib, prec, fwd_tol, bwd_tol):
     tools = more_tools()
     sc = small_scene(n=3000, tools=tools, precision=prec)
@@ -450,7 +471,8 @@ def test_collision_trajectory_loss_and_grad(gpu_lib):
     assert rel_err(g, grad_ref) < 1e-8
 
 
-@pytest.mark.parametrize("prec,loss_tol,grad_tol", [("fp64", 1e-9, 1e-6), ("fp32_svd64", 1e-3, 5e-2)])
+@pytest.mark.parametrize("prec,loss_tol,grad_tol", [("fp64", 1e-9, 1e-6), ("fp32_svd64", 1e-5, 1e-3),
+                                                    ("fp32", 1e-5, 1e-3)])
 def test_config4_grid128_knife_gripper_trajectory(gpu_lib, prec, loss_tol, grad_tol):
     """Config-4 shape on the 128^3 grid: knife (box ∩ prism) and gripper, density
     L1 to the two half piles plus the soft contact term, against the oracle."""
