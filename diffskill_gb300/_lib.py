@@ -12,7 +12,7 @@ from typing import Optional
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmpm_gb300.so")
 
-ABI_VERSION = 4
+ABI_VERSION = 5
 MPM_OK = 0
 STATUS_OUT_OF_GRID = 1
 STATUS_NONFINITE = 2
@@ -55,7 +55,8 @@ class MpmRenderView(ctypes.Structure):
 
 
 class MpmTuning(ctypes.Structure):
-    _fields_ = [("p2g_ctas", _i32), ("g2p_adj_ctas", _i32), ("p2g_adj_ctas", _i32), ("grid_ctas_per_sm", _i32)]
+    _fields_ = [("p2g_ctas", _i32), ("g2p_adj_ctas", _i32), ("p2g_adj_ctas", _i32), ("grid_ctas_per_sm", _i32),
+                ("g2p_ctas", _i32), ("grid_op_adj_ctas", _i32)]
 
 
 class MpmGridStore(ctypes.Structure):

@@ -36,6 +36,8 @@ CANDIDATES: Dict[str, Sequence[int]] = {
     "g2p_adj_ctas": (6, 5, 7, 8),
     "p2g_adj_ctas": (5, 4, 6),
     "grid_ctas_per_sm": (16, 8, 32),
+    "g2p_ctas": (8, 10, 12),
+    "grid_op_adj_ctas": (6, 12, 16),
 }
 # the profiler kinds (diffskill_gb300._lib.KERNEL_KINDS) each field is judged by
 KINDS: Dict[str, Sequence[str]] = {
@@ -43,8 +45,10 @@ KINDS: Dict[str, Sequence[str]] = {
     "g2p_adj_ctas": ("g2p_adj",),
     "p2g_adj_ctas": ("p2g_adj",),
     "grid_ctas_per_sm": ("grid_op", "grid_op_adj"),
+    "g2p_ctas": ("g2p",),
+    "grid_op_adj_ctas": ("grid_op_adj",),
 }
-FP32_ONLY = ("p2g_ctas", "g2p_adj_ctas", "p2g_adj_ctas")
+FP32_ONLY = ("p2g_ctas", "g2p_adj_ctas", "p2g_adj_ctas", "g2p_ctas", "grid_op_adj_ctas")
 
 
 @dataclass
@@ -53,6 +57,8 @@ class Tuning:
     g2p_adj_ctas: int = 6
     p2g_adj_ctas: int = 5
     grid_ctas_per_sm: int = 16
+    g2p_ctas: int = 8
+    grid_op_adj_ctas: int = 6
     resort_every: Optional[int] = None  # substeps; None = the Horizon's default (one action)
     measured: Dict[str, Dict[str, float]] = field(default_factory=dict)  # candidate -> median ms
 

@@ -60,8 +60,25 @@ cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* st1, c
       MPM_LAUNCH(L, MPM_K_G2P_ADJ, k_g2p_adj<T>, pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
     }
   }
-  MPM_LAUNCH(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, gb, 64, c, L.active, counter, gin, g_gout, g_gin, tools_t,
-             poses_t, L.tool_off, g_pose_f, g_pose_f1);
+  {
+    // FP32: the CTAs-per-SM variant the tuning selects
+    const int v = L.tune.grid_op_adj_ctas;
+    if constexpr (sizeof(T) == 4) {
+      if (v == 12)
+        MPM_LAUNCH(L, MPM_K_GRID_OP_ADJ, (k_grid_op_adj<T, 12>), gb, 64, c, L.active, counter, gin, g_gout, g_gin,
+                   tools_t, poses_t, L.tool_off, g_pose_f, g_pose_f1);
+      else if (v == 16)
+        MPM_LAUNCH(L, MPM_K_GRID_OP_ADJ, (k_grid_op_adj<T, 16>), gb, 64, c, L.active, counter, gin, g_gout, g_gin,
+                   tools_t, poses_t, L.tool_off, g_pose_f, g_pose_f1);
+      else
+        MPM_LAUNCH(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, gb, 64, c, L.active, counter, gin, g_gout, g_gin, tools_t,
+                   poses_t, L.tool_off, g_pose_f, g_pose_f1);
+    } else {
+      (void)v;
+      MPM_LAUNCH(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, gb, 64, c, L.active, counter, gin, g_gout, g_gin, tools_t,
+                 poses_t, L.tool_off, g_pose_f, g_pose_f1);
+    }
+  }
   if (c.n_particles > 0) {
     const int v = L.tune.p2g_adj_ctas;
     if constexpr (sizeof(T) == 4 && sizeof(S) == 4) {

@@ -25,7 +25,7 @@ struct MpmHandle {
   MpmToolDesc* d_tools = nullptr;
   int n_tools = 0;
   bool chained = false;           // mpm_set_chained
-  MpmTuning tune = {0, 0, 0, 0};  // mpm_set_tuning
+  MpmTuning tune = {0, 0, 0, 0, 0, 0};  // mpm_set_tuning
   const void* premarked = nullptr;  // frame whose block flags the last forward g2p set
   std::vector<MpmToolDesc> h_tools;
   unsigned int* d_status = nullptr;
@@ -481,6 +481,9 @@ int mpm_set_tuning(MpmHandle* h, const MpmTuning* t) {
     return fail(h, MPM_E_INVALID, "mpm_set_tuning: p2g_adj_ctas must be 0, 4, 5 or 6");
   if (t->grid_ctas_per_sm != 0 && (t->grid_ctas_per_sm < 2 || t->grid_ctas_per_sm > 64))
     return fail(h, MPM_E_INVALID, "mpm_set_tuning: grid_ctas_per_sm must be 0 or in [2, 64]");
+  if (!in(t->g2p_ctas, {0, 8, 10, 12})) return fail(h, MPM_E_INVALID, "mpm_set_tuning: g2p_ctas must be 0, 8, 10 or 12");
+  if (!in(t->grid_op_adj_ctas, {0, 6, 12, 16}))
+    return fail(h, MPM_E_INVALID, "mpm_set_tuning: grid_op_adj_ctas must be 0, 6, 12 or 16");
   h->tune = *t;
   return MPM_OK;
 }
@@ -492,6 +495,8 @@ int mpm_get_tuning(MpmHandle* h, MpmTuning* t) {
   if (!t->g2p_adj_ctas) t->g2p_adj_ctas = 6;
   if (!t->p2g_adj_ctas) t->p2g_adj_ctas = 5;
   if (!t->grid_ctas_per_sm) t->grid_ctas_per_sm = 16;
+  if (!t->g2p_ctas) t->g2p_ctas = 8;
+  if (!t->grid_op_adj_ctas) t->grid_op_adj_ctas = 6;
   return MPM_OK;
 }
 

@@ -131,9 +131,23 @@ cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const d
   MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3), 64, c, L.active,
              counter, gin, gout, (const Tool<T>*)L.tools_t, (const T*)L.poses_t, L.tool_off,
              store ? *store : MpmGridStore{}, store ? slot : -1, (const int64_t*)nullptr);
-  if (c.n_particles > 0)
-    MPM_LAUNCH(L, MPM_K_G2P, k_g2p<T>, blocks_for(c.n_particles, 128), 128, c, st0, st1, L.pscene, gout,
-               mark_next ? L.blockbuf + 16 : (unsigned char*)nullptr, reinterpret_cast<int*>(L.blockbuf));
+  if (c.n_particles > 0) {
+    const unsigned pb = blocks_for(c.n_particles, 128);
+    unsigned char* mark = mark_next ? L.blockbuf + 16 : (unsigned char*)nullptr;
+    int* header = reinterpret_cast<int*>(L.blockbuf);
+    const int v = L.tune.g2p_ctas;
+    if constexpr (sizeof(T) == 4) {
+      if (v == 10)
+        MPM_LAUNCH(L, MPM_K_G2P, (k_g2p<T, 10>), pb, 128, c, st0, st1, L.pscene, gout, mark, header);
+      else if (v == 12)
+        MPM_LAUNCH(L, MPM_K_G2P, (k_g2p<T, 12>), pb, 128, c, st0, st1, L.pscene, gout, mark, header);
+      else
+        MPM_LAUNCH(L, MPM_K_G2P, k_g2p<T>, pb, 128, c, st0, st1, L.pscene, gout, mark, header);
+    } else {
+      (void)v;
+      MPM_LAUNCH(L, MPM_K_G2P, k_g2p<T>, pb, 128, c, st0, st1, L.pscene, gout, mark, header);
+    }
+  }
   return cudaGetLastError();
 }
 

@@ -1025,8 +1025,10 @@ MPM_DI bool g2p_particle(const Consts<T>& c, const T* __restrict__ st, T* __rest
 // stencils of the new positions touch, for the next substep, whose
 // compaction reads them instead of a marking pass; header[0..1] (list length,
 // reservation ticket) are reset for that substep.
-template <typename T>
-__global__ void __launch_bounds__(128) k_g2p(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
+// At least MB CTAs of 128 threads per SM (MpmTuning.g2p_ctas; 0 = 8 in FP32:
+// at most 64 registers)
+template <typename T, int MB = 0>
+__global__ void __launch_bounds__(128, MB > 0 ? MB : (sizeof(T) == 4 ? 8 : 1)) k_g2p(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
                                              const int* __restrict__ pscene, const Node<T>* __restrict__ grid,
                                              unsigned char* __restrict__ mark, int* __restrict__ header) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1275,8 +1277,10 @@ MPM_DI T warp_reduce_scatter16(T (&v)[16], int& k) {
   return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(64) k_grid_op_adj(Consts<T> c, const int* __restrict__ active,
+// At least MB CTAs of 64 threads per SM (MpmTuning.grid_op_adj_ctas; 0 = 6:
+// at most 168 registers)
+template <typename T, int MB = 0>
+__global__ void __launch_bounds__(64, MB > 0 ? MB : (sizeof(T) == 4 ? 6 : 1)) k_grid_op_adj(Consts<T> c, const int* __restrict__ active,
                                                     const int* __restrict__ n_active,
                                                     const Node<T>* __restrict__ grid_in,
                                                     const Node<T>* __restrict__ g_grid, Node<T>* __restrict__ g_in,

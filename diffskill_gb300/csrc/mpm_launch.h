@@ -49,7 +49,7 @@ struct LaunchCtx {
   cudaStream_t stream;
   int64_t* launches;           // launch counter
   Profiler* prof;              // may be null
-  MpmTuning tune = {0, 0, 0, 0};  // launch shapes (mpm_set_tuning); 0 = default
+  MpmTuning tune = {0, 0, 0, 0, 0, 0};  // launch shapes (mpm_set_tuning); 0 = default
 };
 
 // launch helper: counts and (optionally) times one kernel launch

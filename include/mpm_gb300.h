@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define MPM_ABI_VERSION 4
+#define MPM_ABI_VERSION 5
 
 /* return codes */
 #define MPM_OK 0
@@ -132,6 +132,9 @@ typedef struct MpmTuning {
   int32_t g2p_adj_ctas;      /* FP32 g2p.grad: 5, 6 (default), 7 or 8 */
   int32_t p2g_adj_ctas;      /* FP32 p2g.grad: 4, 5 (default) or 6 */
   int32_t grid_ctas_per_sm;  /* grid_op / grid_op.grad: 2 .. 64 (default 16) */
+  int32_t g2p_ctas;          /* FP32 g2p: 8 (default: the compiler's 64 registers), 10 or 12 */
+  int32_t grid_op_adj_ctas;  /* FP32 grid_op.grad, CTAs of 64 threads: 6 (default: the compiler's choice),
+                                12 or 16 */
 } MpmTuning;
 
 typedef struct MpmHandle MpmHandle;

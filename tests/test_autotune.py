@@ -13,7 +13,8 @@ def test_pick_keeps_the_current_choice_within_the_margin():
 
 
 def test_coordinate_descent_finds_each_fields_optimum():
-    best = {"p2g_ctas": 8, "g2p_adj_ctas": 5, "p2g_adj_ctas": 5, "grid_ctas_per_sm": 32}
+    best = {"p2g_ctas": 8, "g2p_adj_ctas": 5, "p2g_adj_ctas": 5, "grid_ctas_per_sm": 32, "g2p_ctas": 10,
+            "grid_op_adj_ctas": 6}
     rng = np.random.default_rng(0)
     calls = []
 
@@ -24,7 +25,8 @@ def test_coordinate_descent_finds_each_fields_optimum():
             return base * (1 + 0.05 * abs(shapes[f] - best[f])) * (1 + 0.002 * rng.standard_normal())
         return {"p2g": t("p2g_ctas", 100.0), "g2p_adj": t("g2p_adj_ctas", 120.0),
                 "p2g_adj": t("p2g_adj_ctas", 110.0), "grid_op": t("grid_ctas_per_sm", 10.0),
-                "grid_op_adj": t("grid_ctas_per_sm", 25.0), "clear": 9.0}
+                "grid_op_adj": t("grid_ctas_per_sm", 25.0) * t("grid_op_adj_ctas", 1.0),
+                "g2p": t("g2p_ctas", 50.0), "clear": 9.0}
 
     start = at.Tuning().shapes()
     shapes, seen = at.coordinate_descent(measure, start, reps=3, margin=0.01)
