@@ -36,28 +36,28 @@ cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* st1, c
     // with a grid store the recompute usually exits at once: a grid of one
     // wave of CTAs that stride over the particles
     const unsigned cap = (unsigned)(L.sm_count * 6);
-    MPM_LAUNCH(L, MPM_K_P2G_RECOMP, (k_p2g<T, S, true>), store && pb > cap ? cap : pb, 128, c, st0, (T*)nullptr,
+    MPM_LAUNCH_PDL(L, MPM_K_P2G_RECOMP, (k_p2g<T, S, true>), store && pb > cap ? cap : pb, 128, c, st0, (T*)nullptr,
                L.pscene, gin, saved);
   }
   const Tool<T>* tools_t = (const Tool<T>*)L.tools_t;
   const T* poses_t = (const T*)L.poses_t;
-  MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, gb, 64, c, L.active, counter, gin, gout, tools_t, poses_t, L.tool_off,
+  MPM_LAUNCH_PDL(L, MPM_K_GRID_OP, k_grid_op<T>, gb, 64, c, L.active, counter, gin, gout, tools_t, poses_t, L.tool_off,
              MpmGridStore{}, -1, saved);
   if (c.n_particles > 0) {
     // FP32: the CTAs-per-SM variant the tuning selects
     const int v = L.tune.g2p_adj_ctas;
     if constexpr (sizeof(T) == 4) {
       if (v == 5)
-        MPM_LAUNCH(L, MPM_K_G2P_ADJ, (k_g2p_adj<T, 5>), pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
+        MPM_LAUNCH_PDL(L, MPM_K_G2P_ADJ, (k_g2p_adj<T, 5>), pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
       else if (v == 7)
-        MPM_LAUNCH(L, MPM_K_G2P_ADJ, (k_g2p_adj<T, 7>), pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
+        MPM_LAUNCH_PDL(L, MPM_K_G2P_ADJ, (k_g2p_adj<T, 7>), pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
       else if (v == 8)
-        MPM_LAUNCH(L, MPM_K_G2P_ADJ, (k_g2p_adj<T, 8>), pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
+        MPM_LAUNCH_PDL(L, MPM_K_G2P_ADJ, (k_g2p_adj<T, 8>), pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
       else
-        MPM_LAUNCH(L, MPM_K_G2P_ADJ, k_g2p_adj<T>, pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
+        MPM_LAUNCH_PDL(L, MPM_K_G2P_ADJ, k_g2p_adj<T>, pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
     } else {
       (void)v;
-      MPM_LAUNCH(L, MPM_K_G2P_ADJ, k_g2p_adj<T>, pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
+      MPM_LAUNCH_PDL(L, MPM_K_G2P_ADJ, k_g2p_adj<T>, pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
     }
   }
   {
@@ -65,17 +65,17 @@ cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* st1, c
     const int v = L.tune.grid_op_adj_ctas;
     if constexpr (sizeof(T) == 4) {
       if (v == 12)
-        MPM_LAUNCH(L, MPM_K_GRID_OP_ADJ, (k_grid_op_adj<T, 12>), gb, 64, c, L.active, counter, gin, g_gout, g_gin,
+        MPM_LAUNCH_PDL(L, MPM_K_GRID_OP_ADJ, (k_grid_op_adj<T, 12>), gb, 64, c, L.active, counter, gin, g_gout, g_gin,
                    tools_t, poses_t, L.tool_off, g_pose_f, g_pose_f1);
       else if (v == 16)
-        MPM_LAUNCH(L, MPM_K_GRID_OP_ADJ, (k_grid_op_adj<T, 16>), gb, 64, c, L.active, counter, gin, g_gout, g_gin,
+        MPM_LAUNCH_PDL(L, MPM_K_GRID_OP_ADJ, (k_grid_op_adj<T, 16>), gb, 64, c, L.active, counter, gin, g_gout, g_gin,
                    tools_t, poses_t, L.tool_off, g_pose_f, g_pose_f1);
       else
-        MPM_LAUNCH(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, gb, 64, c, L.active, counter, gin, g_gout, g_gin, tools_t,
+        MPM_LAUNCH_PDL(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, gb, 64, c, L.active, counter, gin, g_gout, g_gin, tools_t,
                    poses_t, L.tool_off, g_pose_f, g_pose_f1);
     } else {
       (void)v;
-      MPM_LAUNCH(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, gb, 64, c, L.active, counter, gin, g_gout, g_gin, tools_t,
+      MPM_LAUNCH_PDL(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, gb, 64, c, L.active, counter, gin, g_gout, g_gin, tools_t,
                  poses_t, L.tool_off, g_pose_f, g_pose_f1);
     }
   }
@@ -83,14 +83,14 @@ cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* st1, c
     const int v = L.tune.p2g_adj_ctas;
     if constexpr (sizeof(T) == 4 && sizeof(S) == 4) {
       if (v == 4)
-        MPM_LAUNCH(L, MPM_K_P2G_ADJ, (k_p2g_adj<T, S, 4>), pb, 128, c, st0, g1, g0, L.pscene, g_gin);
+        MPM_LAUNCH_PDL(L, MPM_K_P2G_ADJ, (k_p2g_adj<T, S, 4>), pb, 128, c, st0, g1, g0, L.pscene, g_gin);
       else if (v == 6)
-        MPM_LAUNCH(L, MPM_K_P2G_ADJ, (k_p2g_adj<T, S, 6>), pb, 128, c, st0, g1, g0, L.pscene, g_gin);
+        MPM_LAUNCH_PDL(L, MPM_K_P2G_ADJ, (k_p2g_adj<T, S, 6>), pb, 128, c, st0, g1, g0, L.pscene, g_gin);
       else
-        MPM_LAUNCH(L, MPM_K_P2G_ADJ, (k_p2g_adj<T, S>), pb, 128, c, st0, g1, g0, L.pscene, g_gin);
+        MPM_LAUNCH_PDL(L, MPM_K_P2G_ADJ, (k_p2g_adj<T, S>), pb, 128, c, st0, g1, g0, L.pscene, g_gin);
     } else {
       (void)v;
-      MPM_LAUNCH(L, MPM_K_P2G_ADJ, (k_p2g_adj<T, S>), pb, 128, c, st0, g1, g0, L.pscene, g_gin);
+      MPM_LAUNCH_PDL(L, MPM_K_P2G_ADJ, (k_p2g_adj<T, S>), pb, 128, c, st0, g1, g0, L.pscene, g_gin);
     }
   }
   return cudaGetLastError();

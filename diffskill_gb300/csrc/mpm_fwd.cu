@@ -66,12 +66,12 @@ cudaError_t prepare_blocks(const LaunchCtx& L, const Consts<T>& c, const T* st, 
   MpmGridStore rst{};
   if (restore) rst = *restore;
   if (!premarked || restore)
-    MPM_LAUNCH(L, MPM_K_CLEAR, k_mark_or_restore<T>, mb, 256, c, st, L.pscene, flags, counter, rst,
+    MPM_LAUNCH_PDL(L, MPM_K_CLEAR, k_mark_or_restore<T>, mb, 256, c, st, L.pscene, flags, counter, rst,
                restore ? restore_slot : -1, L.active, a, a_out, b);
   MpmGridStore rs{};
   if (reserve) rs = *reserve;
   const PoseTableArgs tt{L.n_tools, pose_f, pose_f1, L.poses_t};
-  MPM_LAUNCH(L, MPM_K_CLEAR, k_compact_clear<T>, blocks_for(total, 256), 256, flags, total, L.active, counter, ticket,
+  MPM_LAUNCH_PDL(L, MPM_K_CLEAR, k_compact_clear<T>, blocks_for(total, 256), 256, flags, total, L.active, counter, ticket,
              a, b, saved, rs, reserve ? reserve_slot : -1, tt);
   return cudaGetLastError();
 }
@@ -118,17 +118,17 @@ cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const d
     const int v = L.tune.p2g_ctas;
     if constexpr (sizeof(T) == 4 && sizeof(S) == 4) {
       if (v == 6)
-        MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S, false, 6>), pb, 128, c, st0, st1, L.pscene, gin, none);
+        MPM_LAUNCH_PDL(L, MPM_K_P2G, (k_p2g<T, S, false, 6>), pb, 128, c, st0, st1, L.pscene, gin, none);
       else if (v == 8)
-        MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S, false, 8>), pb, 128, c, st0, st1, L.pscene, gin, none);
+        MPM_LAUNCH_PDL(L, MPM_K_P2G, (k_p2g<T, S, false, 8>), pb, 128, c, st0, st1, L.pscene, gin, none);
       else
-        MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S>), pb, 128, c, st0, st1, L.pscene, gin, none);
+        MPM_LAUNCH_PDL(L, MPM_K_P2G, (k_p2g<T, S>), pb, 128, c, st0, st1, L.pscene, gin, none);
     } else {
       (void)v;
-      MPM_LAUNCH(L, MPM_K_P2G, (k_p2g<T, S>), pb, 128, c, st0, st1, L.pscene, gin, none);
+      MPM_LAUNCH_PDL(L, MPM_K_P2G, (k_p2g<T, S>), pb, 128, c, st0, st1, L.pscene, gin, none);
     }
   }
-  MPM_LAUNCH(L, MPM_K_GRID_OP, k_grid_op<T>, grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3), 64, c, L.active,
+  MPM_LAUNCH_PDL(L, MPM_K_GRID_OP, k_grid_op<T>, grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3), 64, c, L.active,
              counter, gin, gout, (const Tool<T>*)L.tools_t, (const T*)L.poses_t, L.tool_off,
              store ? *store : MpmGridStore{}, store ? slot : -1, (const int64_t*)nullptr);
   if (c.n_particles > 0) {
@@ -138,14 +138,14 @@ cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const d
     const int v = L.tune.g2p_ctas;
     if constexpr (sizeof(T) == 4) {
       if (v == 10)
-        MPM_LAUNCH(L, MPM_K_G2P, (k_g2p<T, 10>), pb, 128, c, st0, st1, L.pscene, gout, mark, header);
+        MPM_LAUNCH_PDL(L, MPM_K_G2P, (k_g2p<T, 10>), pb, 128, c, st0, st1, L.pscene, gout, mark, header);
       else if (v == 12)
-        MPM_LAUNCH(L, MPM_K_G2P, (k_g2p<T, 12>), pb, 128, c, st0, st1, L.pscene, gout, mark, header);
+        MPM_LAUNCH_PDL(L, MPM_K_G2P, (k_g2p<T, 12>), pb, 128, c, st0, st1, L.pscene, gout, mark, header);
       else
-        MPM_LAUNCH(L, MPM_K_G2P, k_g2p<T>, pb, 128, c, st0, st1, L.pscene, gout, mark, header);
+        MPM_LAUNCH_PDL(L, MPM_K_G2P, k_g2p<T>, pb, 128, c, st0, st1, L.pscene, gout, mark, header);
     } else {
       (void)v;
-      MPM_LAUNCH(L, MPM_K_G2P, k_g2p<T>, pb, 128, c, st0, st1, L.pscene, gout, mark, header);
+      MPM_LAUNCH_PDL(L, MPM_K_G2P, k_g2p<T>, pb, 128, c, st0, st1, L.pscene, gout, mark, header);
     }
   }
   return cudaGetLastError();

@@ -75,6 +75,16 @@ MPM_DI void atomic_add_node3(Node<double>* n, double a, double b, double c) {
 // L2 prefetch of the line holding p (no register, no wait)
 MPM_DI void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
+// Programmatic dependent launch (griddepcontrol).  A kernel launched with
+// programmatic stream serialization may start while the kernel before it in
+// the stream is still running: pdl_wait() returns once that kernel has
+// completed and its writes are visible (at once after a plain launch), so a
+// thread reads nothing that kernel writes, and writes nothing it reads,
+// before its pdl_wait().  pdl_trigger() lets the CTAs of the dependent kernel
+// launch from then on (they take SMs this kernel's tail leaves idle).
+MPM_DI void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+MPM_DI void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // quadratic B-spline stencil (mpm_simulator.py:201-204); base truncates like
 // ti.cast(int)
 template <typename T>
@@ -742,6 +752,8 @@ MPM_DI void p2g_chunk(const Consts<T>& c, const T* __restrict__ st, T* __restric
   } else {
     seg = warp_segments(key);
   }
+  pdl_wait();  // the grid blocks are zeroed by the compaction before
+  pdl_trigger();
   T cx[3] = {pm[0], pm[1], pm[2]};
 #pragma unroll 1
   for (int ox = 0; ox < 3; ++ox) {
@@ -792,7 +804,10 @@ template <typename T, typename S, bool Strided = false, int MB = 0>
 __global__ void __launch_bounds__(128, MB > 0 ? MB : ((sizeof(T) == 4 && sizeof(S) == 4) ? 7 : 4)) k_p2g(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
                                              const int* __restrict__ pscene, Node<T>* __restrict__ grid,
                                              const int64_t* __restrict__ saved) {
-  if (saved && *saved >= 0) return;  // the grid of this substep was restored from the grid store
+  if (saved && *saved >= 0) {  // the grid of this substep was restored from the grid store
+    pdl_wait();  // completes only after the kernel before it (dependent launches chain through it)
+    return;
+  }
   if constexpr (Strided) {
     for (int64_t p0 = (int64_t)blockIdx.x * blockDim.x; p0 < c.n_particles; p0 += (int64_t)gridDim.x * blockDim.x)
       p2g_chunk<T, S>(c, st, st_out, pscene, grid, p0 + threadIdx.x);
@@ -932,6 +947,8 @@ __global__ void __launch_bounds__(64) k_grid_op(Consts<T> c, const int* __restri
                                                 const Tool<T>* __restrict__ tools_t, const T* __restrict__ poses_t,
                                                 const int* __restrict__ tool_off, MpmGridStore store,
                                                 int store_slot, const int64_t* __restrict__ saved) {
+  pdl_wait();     // the grid is p2g's output
+  pdl_trigger();  // g2p reads its particle rows while the grid is updated
   if (saved && *saved >= 0) return;
   const int na = *n_active;
   const int64_t start = store_slot >= 0 ? store.slot_start[store_slot] : -1;
@@ -980,6 +997,7 @@ MPM_DI bool g2p_particle(const Consts<T>& c, const T* __restrict__ st, T* __rest
   }
   const Node<T>* g = grid + (int64_t)scene * c.G;
   const StencilAddr A = stencil_addr(c, s);
+  pdl_wait();  // the grid is grid_op's output
   // C = k4 sum_o wgt v(o) (o - fx)^T = k4 (m1 - nv fx^T) with m1 = sum_o wgt v(o) o^T:
   // the offsets o are 0, 1, 2, so m1 takes only additions
   T nv[3] = {T(0), T(0), T(0)}, m1[9], nC[9];
@@ -1036,6 +1054,8 @@ __global__ void __launch_bounds__(128, MB > 0 ? MB : (sizeof(T) == 4 ? 8 : 1)) k
   const int scene = valid ? pscene[p] : 0;  // issued with x
   T xn[3] = {T(0), T(0), T(0)};
   const bool moved = valid && g2p_particle(c, st, st_out, p, scene, grid, xn);
+  pdl_wait();  // grid_op reads the header reset below (and lanes without a stencil have not waited)
+  pdl_trigger();
   if (mark) {  // uniform; all lanes take part in the warp's writer election
     Stencil<T> sn;
     zero_stencil(sn);
@@ -1099,6 +1119,8 @@ __global__ void __launch_bounds__(128, MB > 0 ? MB : (sizeof(T) == 4 ? 6 : 2)) k
   const Node<T>* g = grid + off;
   Node<T>* gg = g_grid + off;
   const StencilAddr A = stencil_addr(c, s);
+  pdl_wait();  // the restored (or recomputed) grid and the zeroed g_grid
+  pdl_trigger();
   if (ok) {
     if (!st1) {
 #pragma unroll
@@ -1287,6 +1309,8 @@ __global__ void __launch_bounds__(64, MB > 0 ? MB : (sizeof(T) == 4 ? 6 : 1)) k_
                                                     const Tool<T>* __restrict__ tools_t,
                                                     const T* __restrict__ poses_t, const int* __restrict__ tool_off,
                                                     double* __restrict__ g_pose_f, double* __restrict__ g_pose_f1) {
+  pdl_wait();     // g_grid is g2p.grad's output
+  pdl_trigger();  // p2g.grad recomputes its particles' stress meanwhile
   const int na = *n_active;
   for (int b = blockIdx.x; b < na; b += gridDim.x) {
     const int64_t gb = active[b];
@@ -1380,6 +1404,8 @@ __global__ void __launch_bounds__(128, MB > 0 ? MB : ((sizeof(T) == 4 && sizeof(
   S g_aff[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) g_aff[k] = S(0);
+  pdl_wait();  // g_in is grid_op.grad's output
+  pdl_trigger();
   if (ok) {
     const Node<T>* gg = g_in + (int64_t)scene * c.G;
     const StencilAddr A = stencil_addr(c, s);
@@ -1487,6 +1513,8 @@ __global__ void __launch_bounds__(256) k_mark_or_restore(Consts<T> c, const T* _
                                                          MpmGridStore store, int slot, int* __restrict__ active,
                                                          Node<T>* __restrict__ a, Node<T>* __restrict__ a_out,
                                                          Node<T>* __restrict__ b) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t start = slot >= 0 ? store.slot_start[slot] : -1;
   if (start >= 0) {
@@ -1549,6 +1577,8 @@ __global__ void __launch_bounds__(256) k_compact_clear(unsigned char* __restrict
                                                        unsigned* __restrict__ ticket, Node<T>* __restrict__ a,
                                                        Node<T>* __restrict__ b, const int64_t* __restrict__ saved,
                                                        MpmGridStore store, int reserve_slot, PoseTableArgs pt) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   pose_table_fill<T>(pt, i, (int64_t)gridDim.x * blockDim.x);
   if (saved && *saved >= 0) return;  // list and grid a restored; b zeroed by the restore

@@ -60,6 +60,35 @@ struct LaunchCtx {
     prof_end((L).prof, _slot, (KIND), (L).stream);                     \
     ++*(L).launches;                                                   \
   } while (0)
+// Launch with programmatic stream serialization: the kernel may start while
+// the previous kernel in the stream runs, and calls pdl_wait() before it
+// touches that kernel's data (mpm_kernels.cuh).  A plain launch while the
+// profiler times kernels one by one.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(cudaStream_t s, void (*kernel)(KArgs...), unsigned grid, unsigned block,
+                              Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+#define MPM_LAUNCH_PDL(L, KIND, KERNEL, GRID, BLOCK, ...)                         \
+  do {                                                                            \
+    if ((L).prof && (L).prof->on) {                                               \
+      MPM_LAUNCH(L, KIND, KERNEL, GRID, BLOCK, __VA_ARGS__);                      \
+    } else {                                                                      \
+      cudaError_t _e = launch_pdl((L).stream, KERNEL, (GRID), (BLOCK), __VA_ARGS__); \
+      ++*(L).launches;                                                            \
+      if (_e != cudaSuccess) return _e;                                           \
+    }                                                                             \
+  } while (0)
 #define MPM_MEMSET(L, PTR, BYTES)                                      \
   do {                                                                 \
     int _slot = prof_begin((L).prof, (L).stream);                      \
