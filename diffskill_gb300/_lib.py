@@ -12,7 +12,7 @@ from typing import Optional
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmpm_gb300.so")
 
-ABI_VERSION = 5
+ABI_VERSION = 6
 MPM_OK = 0
 STATUS_OUT_OF_GRID = 1
 STATUS_NONFINITE = 2
@@ -105,10 +105,13 @@ SIGNATURES = {
     "mpm_launch_count": (_i64, [_c_p]),
     "mpm_profile_enable": (_i32, [_c_p, _i32]),
     "mpm_profile_read": (_i32, [_c_p, ctypes.POINTER(_f64), ctypes.POINTER(_i64)]),
+    "mpm_sort_frame": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p]),
+    "mpm_unsort_frame": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p]),
 }
 
 # kernel kinds of mpm_profile_read (MPM_K_* in the header)
-KERNEL_KINDS = ["p2g", "p2g_recompute", "grid_op", "g2p", "g2p_adj", "grid_op_adj", "p2g_adj", "clear", "other"]
+KERNEL_KINDS = ["p2g", "p2g_recompute", "grid_op", "g2p", "g2p_adj", "grid_op_adj", "p2g_adj", "clear", "other",
+                "sort"]
 
 _lib: Optional[ctypes.CDLL] = None
 

@@ -18,7 +18,7 @@ REPO = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "libmpm_gb300.so")
 BUILD_DIR = os.path.join(HERE, "_build")
 SOURCES = ["mpm_capi.cu", "mpm_fwd.cu", "mpm_bwd.cu", "mpm_loss.cu", "mpm_kinematics.cu", "mpm_render.cu",
-           "mpm_static.cu"]
+           "mpm_static.cu", "mpm_sort.cu"]
 # per-file flags: the renderer rounds every FP32 operation on its own (no FMA
 # contraction), as its reference arithmetic does.  The substep kernels flush
 # FP32 subnormals to zero and take FP32 divides and square roots by the fast

@@ -40,6 +40,7 @@ struct MpmHandle {
   int* d_active = nullptr;
   void* d_tools_t = nullptr;  // tools in the compute precision (converted by mpm_set_tools)
   void* d_poses_t = nullptr;  // poses of the current substep in the compute precision
+  mpm::SortScratch sort;      // particle re-sort (mpm_sort_frame)
   int sm_count = 1;
   std::string err;
   int64_t launches = 0;
@@ -127,9 +128,10 @@ int check_device(MpmHandle* h) {
                                       " but device " + std::to_string(dev) + " is current");
   return MPM_OK;
 }
-int check_aligned(MpmHandle* h, const void* ptr, const char* name, bool allow_null = false) {
+int check_aligned(MpmHandle* h, const void* ptr, const char* name, bool allow_null = false, unsigned align = 16) {
   if (!ptr) return allow_null ? MPM_OK : fail(h, MPM_E_INVALID, std::string(name) + " is NULL");
-  if (((uintptr_t)ptr) % 16 != 0) return fail(h, MPM_E_INVALID, std::string(name) + " is not 16-byte aligned");
+  if (((uintptr_t)ptr) % align != 0)
+    return fail(h, MPM_E_INVALID, std::string(name) + " is not " + std::to_string(align) + "-byte aligned");
   return MPM_OK;
 }
 #define MPM_TRY(x)          \
@@ -194,6 +196,11 @@ int mpm_create(const MpmParams* params, const int64_t* scene_offsets, MpmHandle*
   // block flags start clean; every compaction clears the flags it reads
   ok = ok && cudaMemset(h->d_blockbuf, 0, mpm::blockbuf_bytes(p.n_scenes, p.n_grid)) == cudaSuccess;
   ok = ok && cudaMalloc(&h->d_active, nblocks * sizeof(int)) == cudaSuccess;
+  const size_t np = (size_t)std::max<int64_t>(p.n_particles, 1);
+  ok = ok && cudaMalloc(&h->sort.keys_a, np * sizeof(uint32_t)) == cudaSuccess;
+  ok = ok && cudaMalloc(&h->sort.keys_b, np * sizeof(uint32_t)) == cudaSuccess;
+  ok = ok && cudaMalloc(&h->sort.vals_b, np * sizeof(int32_t)) == cudaSuccess;
+  ok = ok && cudaMalloc(&h->sort.hist, mpm::sort_hist_words(p.n_particles) * sizeof(uint32_t)) == cudaSuccess;
   if (ok) cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
   if (h->sm_count < 1) h->sm_count = 1;
   if (!ok) {
@@ -229,6 +236,10 @@ int mpm_destroy(MpmHandle* h) {
   cudaFree(h->d_active);
   cudaFree(h->d_tools_t);
   cudaFree(h->d_poses_t);
+  cudaFree(h->sort.keys_a);
+  cudaFree(h->sort.keys_b);
+  cudaFree(h->sort.vals_b);
+  cudaFree(h->sort.hist);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
   delete h;
   return MPM_OK;
@@ -533,6 +544,55 @@ int mpm_grid_mass(MpmHandle* h, const void* state, void* grid_m, void* stream) {
                       ? mpm::launch_grid_mass<double>(L, (const double*)state, (double*)grid_m)
                       : mpm::launch_grid_mass<float>(L, (const float*)state, (float*)grid_m);
   return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_grid_mass");
+}
+
+namespace {
+// the frames [a, a + 24 ld) and [b, b + 24 ld) share no byte
+bool frames_disjoint(const MpmHandle* h, const void* a, const void* b) {
+  const uintptr_t n = (uintptr_t)(24 * h->p.ld) * real_size(h->p.precision);
+  const uintptr_t x = (uintptr_t)a, y = (uintptr_t)b;
+  return x + n <= y || y + n <= x;
+}
+int check_sortable(MpmHandle* h, const char* fn) {
+  if (h->p.n_particles > (int64_t)INT32_MAX)
+    return fail(h, MPM_E_INVALID, std::string(fn) + ": more than 2^31 - 1 particles");
+  if (mpm::sort_key_bits(h->p.n_scenes, h->p.n_grid) > 32)
+    return fail(h, MPM_E_INVALID, std::string(fn) + ": n_scenes * n_grid^3 must be below 2^32");
+  return MPM_OK;
+}
+}  // namespace
+
+int mpm_sort_frame(MpmHandle* h, const void* src, void* dst, int32_t* perm, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_sort_frame: NULL handle");
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, src, "src"));
+  MPM_TRY(check_aligned(h, dst, "dst"));
+  MPM_TRY(check_aligned(h, perm, "perm", false, 4));  // int32, read one word at a time
+  MPM_TRY(check_sortable(h, "mpm_sort_frame"));
+  if (!frames_disjoint(h, src, dst)) return fail(h, MPM_E_INVALID, "mpm_sort_frame: src and dst overlap");
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e = h->p.precision == MPM_PREC_FP64
+                      ? mpm::launch_sort_frame<double>(L, (const double*)src, (double*)dst, perm, h->sort)
+                      : mpm::launch_sort_frame<float>(L, (const float*)src, (float*)dst, perm, h->sort);
+  if (e != cudaSuccess) return cuda_fail(h, e, "mpm_sort_frame");
+  // same particle set: the block flags a chained forward set for src hold for dst
+  if (h->premarked == src) h->premarked = dst;
+  return MPM_OK;
+}
+
+int mpm_unsort_frame(MpmHandle* h, const void* g_src, void* g_dst, const int32_t* perm, void* stream) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_unsort_frame: NULL handle");
+  MPM_TRY(check_device(h));
+  MPM_TRY(check_aligned(h, g_src, "g_src"));
+  MPM_TRY(check_aligned(h, g_dst, "g_dst"));
+  MPM_TRY(check_aligned(h, perm, "perm", false, 4));  // int32, read one word at a time
+  MPM_TRY(check_sortable(h, "mpm_unsort_frame"));
+  if (!frames_disjoint(h, g_src, g_dst)) return fail(h, MPM_E_INVALID, "mpm_unsort_frame: g_src and g_dst overlap");
+  mpm::LaunchCtx L = ctx(h, stream);
+  cudaError_t e = h->p.precision == MPM_PREC_FP64
+                      ? mpm::launch_unsort_frame<double>(L, (const double*)g_src, (double*)g_dst, perm)
+                      : mpm::launch_unsort_frame<float>(L, (const float*)g_src, (float*)g_dst, perm);
+  return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_unsort_frame");
 }
 
 int mpm_grid_mass_bwd(MpmHandle* h, const void* state, const void* g_grid_m, void* g_state, void* stream) {

@@ -97,6 +97,23 @@ inline cudaError_t launch_pdl(cudaStream_t s, void (*kernel)(KArgs...), unsigned
     if (_e != cudaSuccess) return _e;                                  \
   } while (0)
 
+// Scratch of the particle re-sort (mpm_sort.cu), owned by the handle: two
+// key buffers and one index buffer of n_particles words, and the digit
+// table of sort_hist_words(n_particles) words.
+struct SortScratch {
+  uint32_t* keys_a = nullptr;
+  uint32_t* keys_b = nullptr;
+  int32_t* vals_b = nullptr;
+  uint32_t* hist = nullptr;
+};
+size_t sort_hist_words(int64_t n_particles);
+// bits of the largest sort key ((scene * blocks + block) * 64 + cell)
+int sort_key_bits(int n_scenes, int n_grid);
+template <typename T>
+cudaError_t launch_sort_frame(const LaunchCtx& L, const T* src, T* dst, int32_t* perm, const SortScratch& s);
+template <typename T>
+cudaError_t launch_unsort_frame(const LaunchCtx& L, const T* src, T* dst, const int32_t* perm);
+
 // bytes of the converted tools and of the per-substep pose table (the
 // double-precision sizes cover both precisions)
 size_t tools_t_bytes(int64_t n_tools);

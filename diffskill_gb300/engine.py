@@ -224,6 +224,17 @@ class MpmEngine:
                                                       ctypes.byref(store.struct), slot, _stream()), self.h,
                        "mpm_substep_bwd_store")
 
+    def sort_frame(self, src: torch.Tensor, dst: torch.Tensor, perm: torch.Tensor) -> None:
+        """dst = src with its particles sorted by (scene, 4^3 block, cell), stably;
+        ``perm`` (int32 [P]) receives the order: dst[:, i] = src[:, perm[i]]."""
+        _lib.check(self.lib.mpm_sort_frame(self.h, _ptr(src), _ptr(dst), _ptr(perm), _stream()), self.h,
+                   "mpm_sort_frame")
+
+    def unsort_frame(self, g_src: torch.Tensor, g_dst: torch.Tensor, perm: torch.Tensor) -> None:
+        """Adjoint of ``sort_frame`` on a frame gradient: g_dst[:, perm[i]] = g_src[:, i]."""
+        _lib.check(self.lib.mpm_unsort_frame(self.h, _ptr(g_src), _ptr(g_dst), _ptr(perm), _stream()), self.h,
+                   "mpm_unsort_frame")
+
     def grid_mass(self, st: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         if out is None:
             out = torch.empty((self.S, self.G), dtype=self.dtype, device=self.device)
@@ -485,7 +496,9 @@ class Horizon:
         counts = torch.as_tensor(np.diff(eng.offsets), device=dev)
         self.pscene = torch.repeat_interleave(torch.arange(eng.S, device=dev), counts)
         self.pscene32 = self.pscene.to(torch.int32)
-        self._tmp = torch.empty((N_ROWS, max(eng.P, 1)), dtype=dt, device=dev)
+        # the frame a substep writes before it is re-sorted into its checkpoint
+        self._tmp = torch.empty((N_ROWS, eng.ld), dtype=dt, device=dev)
+        self._perm_tmp = torch.empty(max(eng.P, 1), dtype=torch.int32, device=dev)
 
     def set_resort_every(self, resort_every: int) -> None:
         """Re-sort the particles by cell every ``resort_every`` substeps (a
@@ -499,7 +512,7 @@ class Horizon:
         self.boundaries = list(range(self.R, self.F, self.R)) if self.R else []
         need = (max(len(self.boundaries), 1), max(self.eng.P, 1))
         if self.perms is None or self.perms.shape[0] < need[0]:
-            self.perms = torch.zeros(need, dtype=torch.int64, device=self.eng.device)
+            self.perms = torch.zeros(need, dtype=torch.int32, device=self.eng.device)
 
     def bytes(self) -> int:
         return sum(t.numel() * t.element_size() for t in
@@ -514,35 +527,10 @@ class Horizon:
         """Sort the particles of ``frame`` by (scene, 4^3 block, cell) in place, on
         the device (an initial state: losses and action gradients do not depend
         on the particle order)."""
-        self._sort_frame(frame, None)
-
-    def _sort_frame(self, frame: torch.Tensor, b: Optional[int]) -> None:
-        """Sort the particles of ``frame`` by (scene, 4^3 block, cell) in place;
-        keep the permutation as boundary ``b``'s (unless ``b`` is None)."""
-        eng, P = self.eng, self.eng.P
-        if P == 0:
+        if self.eng.P == 0:
             return
-        n = eng.n_grid
-        nb = n // 4
-        # 32-bit keys (half the radix-sort passes) whenever scene, block and cell fit
-        it = torch.int32 if eng.S * nb ** 3 * 64 < 2 ** 31 else torch.int64
-        base = (frame[0:3, :P] * n - 0.5).to(it).clamp_(0, n - 1)
-        blk = ((base[0] >> 2) * nb + (base[1] >> 2)) * nb + (base[2] >> 2)
-        loc = ((base[0] & 3) << 4) | ((base[1] & 3) << 2) | (base[2] & 3)
-        key = ((self.pscene32 if it == torch.int32 else self.pscene) * (nb ** 3) + blk) * 64 + loc
-        perm = torch.argsort(key)
-        if b is not None:
-            self.perms[b].copy_(perm)
-        torch.index_select(frame[:, :P], 1, perm, out=self._tmp)
-        frame[:, :P].copy_(self._tmp)
-
-    def _unsort_grad(self, g: torch.Tensor, b: int) -> None:
-        """Adjoint of ``_sort_frame``: bring a frame gradient back to the order before boundary ``b``."""
-        P = self.eng.P
-        if P == 0:
-            return
-        self._tmp.copy_(g[:, :P])
-        g[:, :P].index_copy_(1, self.perms[b], self._tmp)
+        self._tmp.copy_(frame)
+        self.eng.sort_frame(self._tmp, frame, self._perm_tmp)
 
     def forward(self, state0: torch.Tensor, actions: torch.Tensor, pose0: Optional[torch.Tensor] = None,
                 keep_grids: bool = True) -> None:
@@ -581,9 +569,13 @@ class Horizon:
                     nxt = self.ckpt[(f + 1) // self.k]
                 else:
                     nxt = self.seg[(f + 1) % 2]
-                eng.substep(cur, nxt, self.pose[f], self.pose[f + 1], store, f)
-                if self.R and (f + 1) % self.R == 0 and f + 1 < self.F:
-                    self._sort_frame(nxt, (f + 1) // self.R - 1)
+                if self.R and (f + 1) % self.R == 0 and f + 1 < self.F and eng.P:
+                    # a re-sort boundary: the substep writes the scratch frame, which is
+                    # sorted into the frame's place (the permutation kept for the adjoint)
+                    eng.substep(cur, self._tmp, self.pose[f], self.pose[f + 1], store, f)
+                    eng.sort_frame(self._tmp, nxt, self.perms[(f + 1) // self.R - 1])
+                else:
+                    eng.substep(cur, nxt, self.pose[f], self.pose[f + 1], store, f)
                 cur = nxt
         finally:
             eng.set_chained(False)
@@ -673,8 +665,10 @@ class Horizon:
                                 self.g_pose[f + 1], store if slot >= 0 else None, slot, st1=st1)
                 cur, nxt = nxt, cur
             f0 = c * k
-            if self.R and f0 > 0 and f0 % self.R == 0:
-                self._unsort_grad(cur, f0 // self.R - 1)
+            if self.R and f0 > 0 and f0 % self.R == 0 and eng.P:
+                # the gradient of frame f0 back in the order substep f0 - 1 produced
+                eng.unsort_frame(cur, nxt, self.perms[f0 // self.R - 1])
+                cur, nxt = nxt, cur
             tools_bwd_upto(f0)
         tools_bwd_upto(0)
         if eng.T:

@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define MPM_ABI_VERSION 5
+#define MPM_ABI_VERSION 6
 
 /* return codes */
 #define MPM_OK 0
@@ -231,6 +231,21 @@ int mpm_substep_bwd_store(MpmHandle* h, const void* state_f, const void* state_f
                           void* g_state_f, const double* pose_f, const double* pose_f1, double* g_pose_f,
                           double* g_pose_f1, const MpmGridStore* store, int32_t slot, void* stream);
 
+/* Particle re-sort (no counterpart in the reference: Taichi scatters into its
+ * dense fields in launch order, mpm_simulator.py:199-225).  Sorts the
+ * particles of frame src by (scene, 4^3 grid block, cell), stably, and
+ * writes the sorted frame (all 24 rows) to dst: dst[:, i] = src[:, perm[i]].
+ * Particles stay inside their scene, so losses and action gradients do not
+ * change.  perm: int32[n_particles] (device, 4-byte aligned) receives the
+ * permutation.  src and dst must not overlap.  Needs n_particles < 2^31 and
+ * n_scenes * n_grid^3 < 2^32 (MPM_E_INVALID otherwise).  The block flags a
+ * chained forward substep set for src are kept for dst.  No allocation;
+ * capturable. */
+int mpm_sort_frame(MpmHandle* h, const void* src, void* dst, int32_t* perm, void* stream);
+/* Adjoint of mpm_sort_frame for a frame gradient: g_dst[:, perm[i]] =
+ * g_src[:, i] (all 24 rows).  g_src and g_dst must not overlap. */
+int mpm_unsort_frame(MpmHandle* h, const void* g_src, void* g_dst, const int32_t* perm, void* stream);
+
 /* compute_grid_m_kernel on a cleared grid (mpm_simulator.py:456-471).
  * grid_m: real[n_scenes][n_grid^3] written. */
 int mpm_grid_mass(MpmHandle* h, const void* state, void* grid_m, void* stream);
@@ -401,7 +416,8 @@ int64_t mpm_launch_count(MpmHandle* h);
 #define MPM_K_P2G_ADJ 6
 #define MPM_K_CLEAR 7        /* grid clears (memset)               */
 #define MPM_K_OTHER 8        /* density, loss, contact, tools       */
-#define MPM_K_COUNT 9
+#define MPM_K_SORT 9         /* particle re-sort and its adjoint    */
+#define MPM_K_COUNT 10
 
 /* No counterpart in the reference (it has no profiler): when enabled, every
  * kernel launched through the handle is bracketed by a CUDA event pair on its
