@@ -104,10 +104,10 @@ def coordinate_descent(measure: Callable[[Dict[str, int]], Dict[str, float]], st
 
 def resort_candidates(n_sub: int, k: int, F: int) -> List[int]:
     """Re-sort intervals (substeps) worth timing: one action (the default), two
-    and five actions, half an action, and never (0); each a multiple of the
-    checkpoint interval ``k`` and shorter than the horizon ``F``."""
+    and five actions, half and a fifth of an action, and never (0); each a
+    multiple of the checkpoint interval ``k`` and shorter than the horizon ``F``."""
     out = []
-    for R in (n_sub, 2 * n_sub, 5 * n_sub, n_sub // 2):
+    for R in (n_sub, 2 * n_sub, 5 * n_sub, n_sub // 2, n_sub // 5):
         R = k * max(1, -(-R // k))
         if 0 < R < F and R not in out:
             out.append(R)

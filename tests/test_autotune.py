@@ -44,11 +44,11 @@ def test_coordinate_descent_leaves_defaults_when_nothing_is_faster():
 
 def test_resort_candidates_respect_the_checkpoint_interval_and_horizon():
     c = at.resort_candidates(50, 1, 1000)
-    assert c == [50, 100, 250, 25, 0]
+    assert c == [50, 100, 250, 25, 10, 0]
     c = at.resort_candidates(50, 10, 1000)
     assert all(r % 10 == 0 for r in c) and c[0] == 50 and c[-1] == 0 and 30 in c
     c = at.resort_candidates(50, 10, 100)  # a two-action horizon: one interior boundary at most
-    assert c == [50, 30, 0]
+    assert c == [50, 30, 10, 0]
 
 
 def test_tuning_cache_round_trip(tmp_path, monkeypatch):
