@@ -211,11 +211,24 @@ struct SlabStage {
   Node<float>* base[32];  // grid of the row's scene + ax[ox] of the row's base cell
   int ay[32][3], az[32][3];
 };
+// Packed FP32 pairs (add/mul/fma .f32x2): one instruction for two lanes of
+// arithmetic, each rounded as the scalar operation would be
+MPM_DI unsigned long long f2_bits(float2 a) { return *reinterpret_cast<unsigned long long*>(&a); }
+MPM_DI float2 f2_of(unsigned long long b) { return *reinterpret_cast<float2*>(&b); }
+MPM_DI float2 add2(float2 a, float2 b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return f2_of(d);
+}
+MPM_DI float2 mul2(float2 a, float2 b) {
+  unsigned long long d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return f2_of(d);
+}
 MPM_DI void f4_add(float4& a, const float4& b) {
-  a.x += b.x;
-  a.y += b.y;
-  a.z += b.z;
-  a.w += b.w;
+  const float2 lo = add2(make_float2(a.x, a.y), make_float2(b.x, b.y));
+  const float2 hi = add2(make_float2(a.z, a.w), make_float2(b.z, b.w));
+  a = make_float4(lo.x, lo.y, hi.x, hi.y);
 }
 MPM_DI float4 f4_shfl_up(const float4& a, int d) {
   return make_float4(__shfl_up_sync(0xffffffffu, a.x, d), __shfl_up_sync(0xffffffffu, a.y, d),
@@ -754,44 +767,70 @@ MPM_DI void p2g_chunk(const Consts<T>& c, const T* __restrict__ st, T* __restric
   }
   pdl_wait();  // the grid blocks are zeroed by the compaction before
   pdl_trigger();
-  T cx[3] = {pm[0], pm[1], pm[2]};
+  if constexpr (slab) {
+    // FP32: the node value wgt (m v + A dp, m) in packed pairs: (x, y) and
+    // (z, m), stepped across the stencil by the columns of A (and 0 for m)
+    float2 cxA = make_float2(pm[0], pm[1]), cxB = make_float2(pm[2], c.p_mass);
+    const float2 a0A = make_float2(affine[0], affine[3]), a0B = make_float2(affine[6], 0.f);
+    const float2 a1A = make_float2(affine[1], affine[4]), a1B = make_float2(affine[7], 0.f);
+    const float2 a2A = make_float2(affine[2], affine[5]), a2B = make_float2(affine[8], 0.f);
 #pragma unroll 1
-  for (int ox = 0; ox < 3; ++ox) {
-    const T wx = sel3(s.w[0][0], s.w[1][0], s.w[2][0], ox);
-    const int ax = sel3(A.ax[0], A.ax[1], A.ax[2], ox);
-    T cy[3] = {cx[0], cx[1], cx[2]};
+    for (int ox = 0; ox < 3; ++ox) {
+      const float wx = sel3(s.w[0][0], s.w[1][0], s.w[2][0], ox);
+      const int ax = sel3(A.ax[0], A.ax[1], A.ax[2], ox);
+      float2 cyA = cxA, cyB = cxB;
 #pragma unroll
-    for (int oy = 0; oy < 3; ++oy) {
-      T cz[3] = {cy[0], cy[1], cy[2]};
+      for (int oy = 0; oy < 3; ++oy) {
+        float2 czA = cyA, czB = cyB;
 #pragma unroll
-      for (int oz = 0; oz < 3; ++oz) {
-        const T wgt = wx * s.w[oy][1] * s.w[oz][2];
-        T mv[4];
+        for (int oz = 0; oz < 3; ++oz) {
+          const float wgt = wx * s.w[oy][1] * s.w[oz][2];
+          const float2 w2 = make_float2(wgt, wgt);
+          const float2 lo = mul2(w2, czA), hi = mul2(w2, czB);
+          sb->v[lane][oy * 3 + oz] = make_float4(lo.x, lo.y, hi.x, hi.y);
+          czA = add2(czA, a2A);
+          czB = add2(czB, a2B);
+        }
+        cyA = add2(cyA, a1A);
+        cyB = add2(cyB, a1B);
+      }
+      cxA = add2(cxA, a0A);
+      cxB = add2(cxB, a0B);
+      sb->base[lane] = g + ax;
+      __syncwarp();
+      slab_reduce(*sb, tails, emit);
+      __syncwarp();
+    }
+  } else {
+    T cx[3] = {pm[0], pm[1], pm[2]};
+#pragma unroll 1
+    for (int ox = 0; ox < 3; ++ox) {
+      const T wx = sel3(s.w[0][0], s.w[1][0], s.w[2][0], ox);
+      const int ax = sel3(A.ax[0], A.ax[1], A.ax[2], ox);
+      T cy[3] = {cx[0], cx[1], cx[2]};
 #pragma unroll
-        for (int k = 0; k < 3; ++k) mv[k] = wgt * cz[k];
-        mv[3] = wgt * c.p_mass;
-        if constexpr (slab) {
-          sb->v[lane][oy * 3 + oz] = make_float4(mv[0], mv[1], mv[2], mv[3]);
-        } else {
+      for (int oy = 0; oy < 3; ++oy) {
+        T cz[3] = {cy[0], cy[1], cy[2]};
+#pragma unroll
+        for (int oz = 0; oz < 3; ++oz) {
+          const T wgt = wx * s.w[oy][1] * s.w[oz][2];
+          T mv[4];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) mv[k] = wgt * cz[k];
+          mv[3] = wgt * c.p_mass;
           if (seg.steps) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) mv[k] = seg_scan(mv[k], seg);
           }
           if (ok && seg.tail) atomic_add_node(g + ax + A.ay[oy] + A.az[oz], mv[0], mv[1], mv[2], mv[3]);
+#pragma unroll
+          for (int k = 0; k < 3; ++k) cz[k] += affine[3 * k + 2];
         }
 #pragma unroll
-        for (int k = 0; k < 3; ++k) cz[k] += affine[3 * k + 2];
+        for (int k = 0; k < 3; ++k) cy[k] += affine[3 * k + 1];
       }
 #pragma unroll
-      for (int k = 0; k < 3; ++k) cy[k] += affine[3 * k + 1];
-    }
-#pragma unroll
-    for (int k = 0; k < 3; ++k) cx[k] += affine[3 * k];
-    if constexpr (slab) {
-      sb->base[lane] = g + ax;
-      __syncwarp();
-      slab_reduce(*sb, tails, emit);
-      __syncwarp();
+      for (int k = 0; k < 3; ++k) cx[k] += affine[3 * k];
     }
   }
 }
