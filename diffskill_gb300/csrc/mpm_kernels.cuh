@@ -225,10 +225,20 @@ MPM_DI float2 mul2(float2 a, float2 b) {
   asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
   return f2_of(d);
 }
+// a += b, in two packed pair additions or four scalar ones (measured: the
+// packed form helps p2g and slows g2p.grad, whose fourth lane is zero)
+template <bool Packed = false>
 MPM_DI void f4_add(float4& a, const float4& b) {
-  const float2 lo = add2(make_float2(a.x, a.y), make_float2(b.x, b.y));
-  const float2 hi = add2(make_float2(a.z, a.w), make_float2(b.z, b.w));
-  a = make_float4(lo.x, lo.y, hi.x, hi.y);
+  if constexpr (Packed) {
+    const float2 lo = add2(make_float2(a.x, a.y), make_float2(b.x, b.y));
+    const float2 hi = add2(make_float2(a.z, a.w), make_float2(b.z, b.w));
+    a = make_float4(lo.x, lo.y, hi.x, hi.y);
+  } else {
+    a.x += b.x;
+    a.y += b.y;
+    a.z += b.z;
+    a.w += b.w;
+  }
 }
 MPM_DI float4 f4_shfl_up(const float4& a, int d) {
   return make_float4(__shfl_up_sync(0xffffffffu, a.x, d), __shfl_up_sync(0xffffffffu, a.y, d),
@@ -238,6 +248,7 @@ MPM_DI void slab_emit(const SlabStage& sb, int r, int oy, int oz, const float4& 
   atomicAdd(reinterpret_cast<float4*>(sb.base[r] + sb.ay[r][oy] + sb.az[r][oz]), a);
 }
 // call between two __syncwarp()s, after all lanes wrote their row of sb.v
+template <bool Packed = false>
 MPM_DI void slab_reduce(const SlabStage& sb, unsigned tails, unsigned emit) {
   const int lane = threadIdx.x & 31;
   // lanes 27..31 (g = 3) read lane 24's cells (a broadcast) and emit nothing
@@ -250,7 +261,7 @@ MPM_DI void slab_reduce(const SlabStage& sb, unsigned tails, unsigned emit) {
   int head_row = -1;
 #pragma unroll
   for (int i = 0; i < 11; ++i) {
-    f4_add(acc, sb.v[r0 + i][j]);
+    f4_add<Packed>(acc, sb.v[r0 + i][j]);
     if ((mine >> i) & 1u) {
       if (g > 0 && head_row < 0) {
         head = acc;  // closes a run that may have started in the group before
@@ -798,7 +809,7 @@ MPM_DI void p2g_chunk(const Consts<T>& c, const T* __restrict__ st, T* __restric
       cxB = add2(cxB, a0B);
       sb->base[lane] = g + ax;
       __syncwarp();
-      slab_reduce(*sb, tails, emit);
+      slab_reduce<true>(*sb, tails, emit);
       __syncwarp();
     }
   } else {
@@ -978,9 +989,11 @@ MPM_DI void walls_vjp(const Consts<T>& c, const int* I, const WallTape<T>& tp, T
 // the grid store at slot_start + b (reserved by the compaction; -1 when the
 // store is full).  saved (may be null; the adjoint's recompute): when it
 // points at a slot start >= 0 both grids were restored from the store and the
-// kernel returns at once.
+// kernel returns at once.  At least 16 CTAs per SM (64 registers, a small
+// spill): with the grid-stride width of 16 CTAs per SM all of them are
+// resident at once (measured 9.8 -> 9.2 us on 32 scenes against 80 registers).
 template <typename T>
-__global__ void __launch_bounds__(64) k_grid_op(Consts<T> c, const int* __restrict__ active,
+__global__ void __launch_bounds__(64, 16) k_grid_op(Consts<T> c, const int* __restrict__ active,
                                                 const int* __restrict__ n_active,
                                                 const Node<T>* __restrict__ grid_in, Node<T>* __restrict__ grid_out,
                                                 const Tool<T>* __restrict__ tools_t, const T* __restrict__ poses_t,
