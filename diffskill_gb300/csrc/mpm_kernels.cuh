@@ -989,11 +989,11 @@ MPM_DI void walls_vjp(const Consts<T>& c, const int* I, const WallTape<T>& tp, T
 // the grid store at slot_start + b (reserved by the compaction; -1 when the
 // store is full).  saved (may be null; the adjoint's recompute): when it
 // points at a slot start >= 0 both grids were restored from the store and the
-// kernel returns at once.  At least 16 CTAs per SM (64 registers, a small
+// kernel returns at once.  FP32: at least 16 CTAs per SM (64 registers, a small
 // spill): with the grid-stride width of 16 CTAs per SM all of them are
 // resident at once (measured 9.8 -> 9.2 us on 32 scenes against 80 registers).
 template <typename T>
-__global__ void __launch_bounds__(64, 16) k_grid_op(Consts<T> c, const int* __restrict__ active,
+__global__ void __launch_bounds__(64, sizeof(T) == 4 ? 16 : 1) k_grid_op(Consts<T> c, const int* __restrict__ active,
                                                 const int* __restrict__ n_active,
                                                 const Node<T>* __restrict__ grid_in, Node<T>* __restrict__ grid_out,
                                                 const Tool<T>* __restrict__ tools_t, const T* __restrict__ poses_t,
