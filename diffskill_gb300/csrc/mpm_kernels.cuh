@@ -983,7 +983,6 @@ MPM_DI void walls_vjp(const Consts<T>& c, const int* I, const WallTape<T>& tp, T
   }
 }
 
-// Per-CTA tool table, reloaded when the block's scene changes.
 // grid_op over the active blocks: one 64-thread CTA per block, grid-stride.
 // store_slot >= 0: list block b of grid_in and of grid_out are also copied to
 // the grid store at slot_start + b (reserved by the compaction; -1 when the
