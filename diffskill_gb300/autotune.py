@@ -39,7 +39,7 @@ CANDIDATES: Dict[str, Sequence[int]] = {
     "g2p_ctas": (8, 10, 12),
     "grid_op_adj_ctas": (6, 12, 16),
 }
-# the profiler kinds (diffskill_gb300._lib.KERNEL_KINDS) each field is judged by
+# the profiler kinds (diffskill_gb300._lib.KERNEL_KINDS) whose times decide each field
 KINDS: Dict[str, Sequence[str]] = {
     "p2g_ctas": ("p2g",),
     "g2p_adj_ctas": ("g2p_adj",),
