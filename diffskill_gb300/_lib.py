@@ -106,6 +106,7 @@ SIGNATURES = {
     "mpm_profile_enable": (_i32, [_c_p, _i32]),
     "mpm_profile_read": (_i32, [_c_p, ctypes.POINTER(_f64), ctypes.POINTER(_i64)]),
     "mpm_sort_frame": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p]),
+    "mpm_set_pipelined_adjoint": (_i32, [_c_p, _i32]),
     "mpm_unsort_frame": (_i32, [_c_p, _c_p, _c_p, _c_p, _c_p]),
 }
 

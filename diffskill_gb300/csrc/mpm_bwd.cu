@@ -18,7 +18,7 @@ static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs
 template <typename T, typename S>
 cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* st1, const T* g1, T* g0,
                                const double* pose_f, const double* pose_f1, double* g_pose_f, double* g_pose_f1,
-                               const MpmGridStore* store, int slot) {
+                               const MpmGridStore* store, int slot, unsigned phases) {
   Consts<T> c = make_consts<T>(L);
   Node<T>* gin = (Node<T>*)L.grid_a;
   Node<T>* gout = (Node<T>*)L.grid_b;
@@ -27,59 +27,72 @@ cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* st1, c
   const int* counter = reinterpret_cast<const int*>(L.blockbuf);
   const unsigned pb = blocks_for(c.n_particles, 128);
   const unsigned gb = grid_blocks_launch(L, (int64_t)c.n_scenes * c.NB3);
-  // recompute the grids of this substep (substep_grad, mpm_simulator.py:327-333)
-  // unless the grid store holds them (then p2g and grid_op return at once)
-  const int64_t* saved = store ? store->slot_start + slot : nullptr;
-  cudaError_t e = prepare_blocks<T>(L, c, st0, gin, gout, g_gout, store, slot, nullptr, -1, pose_f, pose_f1, false);
-  if (e != cudaSuccess) return e;
-  if (c.n_particles > 0) {
-    // with a grid store the recompute usually exits at once: a grid of one
-    // wave of CTAs that stride over the particles
-    const unsigned cap = (unsigned)(L.sm_count * 6);
-    MPM_LAUNCH_PDL(L, MPM_K_P2G_RECOMP, (k_p2g<T, S, true>), store && pb > cap ? cap : pb, 128, c, st0, (T*)nullptr,
-               L.pscene, gin, saved);
-  }
   const Tool<T>* tools_t = (const Tool<T>*)L.tools_t;
   const T* poses_t = (const T*)L.poses_t;
-  MPM_LAUNCH_PDL(L, MPM_K_GRID_OP, k_grid_op<T>, gb, 64, c, L.active, counter, gin, gout, tools_t, poses_t, L.tool_off,
-             MpmGridStore{}, -1, saved);
-  if (c.n_particles > 0) {
-    // FP32: the CTAs-per-SM variant the tuning selects
-    const int v = L.tune.g2p_adj_ctas;
+  if (phases & BWD_PREPARE) {
+    // recompute the grids of this substep (substep_grad, mpm_simulator.py:327-333)
+    // unless the grid store holds them (then p2g and grid_op return at once)
+    const int64_t* saved = store ? store->slot_start + slot : nullptr;
+    cudaError_t e = prepare_blocks<T>(L, c, st0, gin, gout, g_gout, store, slot, nullptr, -1, pose_f, pose_f1, false);
+    if (e != cudaSuccess) return e;
+    if (c.n_particles > 0) {
+      // with a grid store the recompute usually exits at once: a grid of one
+      // wave of CTAs that stride over the particles
+      const unsigned cap = (unsigned)(L.sm_count * 6);
+      MPM_LAUNCH_PDL(L, MPM_K_P2G_RECOMP, (k_p2g<T, S, true>), store && pb > cap ? cap : pb, 128, c, st0,
+                     (T*)nullptr, L.pscene, gin, saved);
+    }
+    MPM_LAUNCH_PDL(L, MPM_K_GRID_OP, k_grid_op<T>, gb, 64, c, L.active, counter, gin, gout, tools_t, poses_t,
+                   L.tool_off, MpmGridStore{}, -1, saved);
+  }
+  if ((phases & BWD_GRID) && c.n_particles > 0) {
+    // FP32: the CTAs-per-SM variant the tuning selects.  BWD_G2P_PLAIN: the
+    // kernel before it in the stream may be the previous substep's p2g.grad,
+    // which writes the rows of g1 that g2p.grad reads before its wait
+    const int v = sizeof(T) == 4 ? L.tune.g2p_adj_ctas : 0;
+    const bool plain = (phases & BWD_G2P_PLAIN) != 0;
+#define MPM_G2P_ADJ(K)                                                                                 \
+  do {                                                                                                 \
+    if (plain)                                                                                         \
+      MPM_LAUNCH(L, MPM_K_G2P_ADJ, K, pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);           \
+    else                                                                                               \
+      MPM_LAUNCH_PDL(L, MPM_K_G2P_ADJ, K, pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);       \
+  } while (0)
     if constexpr (sizeof(T) == 4) {
       if (v == 5)
-        MPM_LAUNCH_PDL(L, MPM_K_G2P_ADJ, (k_g2p_adj<T, 5>), pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
+        MPM_G2P_ADJ((k_g2p_adj<T, 5>));
       else if (v == 7)
-        MPM_LAUNCH_PDL(L, MPM_K_G2P_ADJ, (k_g2p_adj<T, 7>), pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
+        MPM_G2P_ADJ((k_g2p_adj<T, 7>));
       else if (v == 8)
-        MPM_LAUNCH_PDL(L, MPM_K_G2P_ADJ, (k_g2p_adj<T, 8>), pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
+        MPM_G2P_ADJ((k_g2p_adj<T, 8>));
       else
-        MPM_LAUNCH_PDL(L, MPM_K_G2P_ADJ, k_g2p_adj<T>, pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
+        MPM_G2P_ADJ(k_g2p_adj<T>);
     } else {
       (void)v;
-      MPM_LAUNCH_PDL(L, MPM_K_G2P_ADJ, k_g2p_adj<T>, pb, 128, c, st0, st1, g1, g0, L.pscene, gout, g_gout);
+      MPM_G2P_ADJ(k_g2p_adj<T>);
     }
+#undef MPM_G2P_ADJ
   }
-  {
+  if (phases & BWD_GRID) {
     // FP32: the CTAs-per-SM variant the tuning selects
     const int v = L.tune.grid_op_adj_ctas;
     if constexpr (sizeof(T) == 4) {
       if (v == 12)
         MPM_LAUNCH_PDL(L, MPM_K_GRID_OP_ADJ, (k_grid_op_adj<T, 12>), gb, 64, c, L.active, counter, gin, g_gout, g_gin,
-                   tools_t, poses_t, L.tool_off, g_pose_f, g_pose_f1);
+                       tools_t, poses_t, L.tool_off, g_pose_f, g_pose_f1);
       else if (v == 16)
         MPM_LAUNCH_PDL(L, MPM_K_GRID_OP_ADJ, (k_grid_op_adj<T, 16>), gb, 64, c, L.active, counter, gin, g_gout, g_gin,
-                   tools_t, poses_t, L.tool_off, g_pose_f, g_pose_f1);
+                       tools_t, poses_t, L.tool_off, g_pose_f, g_pose_f1);
       else
-        MPM_LAUNCH_PDL(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, gb, 64, c, L.active, counter, gin, g_gout, g_gin, tools_t,
-                   poses_t, L.tool_off, g_pose_f, g_pose_f1);
+        MPM_LAUNCH_PDL(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, gb, 64, c, L.active, counter, gin, g_gout, g_gin,
+                       tools_t, poses_t, L.tool_off, g_pose_f, g_pose_f1);
     } else {
       (void)v;
       MPM_LAUNCH_PDL(L, MPM_K_GRID_OP_ADJ, k_grid_op_adj<T>, gb, 64, c, L.active, counter, gin, g_gout, g_gin, tools_t,
-                 poses_t, L.tool_off, g_pose_f, g_pose_f1);
+                     poses_t, L.tool_off, g_pose_f, g_pose_f1);
     }
   }
-  if (c.n_particles > 0) {
+  if ((phases & BWD_PARTICLES) && c.n_particles > 0) {
     const int v = L.tune.p2g_adj_ctas;
     if constexpr (sizeof(T) == 4 && sizeof(S) == 4) {
       if (v == 4)
@@ -218,7 +231,7 @@ template cudaError_t launch_tool_distance_bwd<double>(const LaunchCtx&, const in
 
 #define MPM_INST_BWD(T, S)                                                                                  \
   template cudaError_t launch_substep_bwd<T, S>(const LaunchCtx&, const T*, const T*, const T*, T*, const double*, \
-                                                const double*, double*, double*, const MpmGridStore*, int);
+                                                const double*, double*, double*, const MpmGridStore*, int, unsigned);
 MPM_INST_BWD(float, float)
 MPM_INST_BWD(float, double)
 MPM_INST_BWD(double, double)

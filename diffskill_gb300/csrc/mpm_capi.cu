@@ -41,6 +41,14 @@ struct MpmHandle {
   void* d_tools_t = nullptr;  // tools in the compute precision (converted by mpm_set_tools)
   void* d_poses_t = nullptr;  // poses of the current substep in the compute precision
   mpm::SortScratch sort;      // particle re-sort (mpm_sort_frame)
+  // pipelined adjoint (mpm_set_pipelined_adjoint): the grid preparation of an
+  // adjoint substep runs on pipe_side beside the previous substep's p2g.grad
+  bool pipelined = false;
+  bool pipe_pending = false;          // the last call was a pipelined adjoint substep on pipe_stream
+  void* pipe_stream = nullptr;
+  cudaStream_t pipe_side = nullptr;
+  cudaEvent_t pipe_grid_done = nullptr;  // recorded after grid_op.grad of the last call
+  cudaEvent_t pipe_prep_done = nullptr;  // recorded after the side stream's preparation
   int sm_count = 1;
   std::string err;
   int64_t launches = 0;
@@ -201,6 +209,10 @@ int mpm_create(const MpmParams* params, const int64_t* scene_offsets, MpmHandle*
   ok = ok && cudaMalloc(&h->sort.keys_b, np * sizeof(uint32_t)) == cudaSuccess;
   ok = ok && cudaMalloc(&h->sort.vals_b, np * sizeof(int32_t)) == cudaSuccess;
   ok = ok && cudaMalloc(&h->sort.hist, mpm::sort_hist_words(p.n_particles) * sizeof(uint32_t)) == cudaSuccess;
+  // the pipelined adjoint's internal stream and events (created here, outside any stream capture)
+  ok = ok && cudaStreamCreateWithFlags(&h->pipe_side, cudaStreamNonBlocking) == cudaSuccess;
+  ok = ok && cudaEventCreateWithFlags(&h->pipe_grid_done, cudaEventDisableTiming) == cudaSuccess;
+  ok = ok && cudaEventCreateWithFlags(&h->pipe_prep_done, cudaEventDisableTiming) == cudaSuccess;
   if (ok) cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
   if (h->sm_count < 1) h->sm_count = 1;
   if (!ok) {
@@ -240,6 +252,9 @@ int mpm_destroy(MpmHandle* h) {
   cudaFree(h->sort.keys_b);
   cudaFree(h->sort.vals_b);
   cudaFree(h->sort.hist);
+  if (h->pipe_side) cudaStreamDestroy(h->pipe_side);
+  if (h->pipe_grid_done) cudaEventDestroy(h->pipe_grid_done);
+  if (h->pipe_prep_done) cudaEventDestroy(h->pipe_prep_done);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
   delete h;
   return MPM_OK;
@@ -412,6 +427,7 @@ static int substep_fwd_impl(MpmHandle* h, const void* state_f, void* state_f1, c
   const bool pre = h->chained && h->premarked == state_f;
   const bool next = h->chained;
   h->premarked = nullptr;
+  h->pipe_pending = false;  // a forward substep rewrites the grids: no adjoint overlaps it
   cudaError_t e;
   switch (h->p.precision) {
     case MPM_PREC_FP32:
@@ -450,24 +466,60 @@ static int substep_bwd_impl(MpmHandle* h, const void* state_f, const void* state
   MPM_TRY(check_store(h, store, slot));
   mpm::LaunchCtx L = ctx(h, stream);
   h->premarked = nullptr;  // the adjoint's compaction may consume the flags
-  cudaError_t e;
-  switch (h->p.precision) {
-    case MPM_PREC_FP32:
-      e = mpm::launch_substep_bwd<float, float>(L, (const float*)state_f, (const float*)state_f1,
-                                                (const float*)g_state_f1, (float*)g_state_f, pose_f, pose_f1,
-                                                g_pose_f, g_pose_f1, store, slot);
-      break;
-    case MPM_PREC_FP32_SVD64:
-      e = mpm::launch_substep_bwd<float, double>(L, (const float*)state_f, (const float*)state_f1,
-                                                 (const float*)g_state_f1, (float*)g_state_f, pose_f, pose_f1,
-                                                 g_pose_f, g_pose_f1, store, slot);
-      break;
-    default:
-      e = mpm::launch_substep_bwd<double, double>(L, (const double*)state_f, (const double*)state_f1,
-                                                  (const double*)g_state_f1, (double*)g_state_f, pose_f, pose_f1,
-                                                  g_pose_f, g_pose_f1, store, slot);
+  auto run = [&](const mpm::LaunchCtx& C, unsigned phases) -> cudaError_t {
+    switch (h->p.precision) {
+      case MPM_PREC_FP32:
+        return mpm::launch_substep_bwd<float, float>(C, (const float*)state_f, (const float*)state_f1,
+                                                     (const float*)g_state_f1, (float*)g_state_f, pose_f, pose_f1,
+                                                     g_pose_f, g_pose_f1, store, slot, phases);
+      case MPM_PREC_FP32_SVD64:
+        return mpm::launch_substep_bwd<float, double>(C, (const float*)state_f, (const float*)state_f1,
+                                                      (const float*)g_state_f1, (float*)g_state_f, pose_f, pose_f1,
+                                                      g_pose_f, g_pose_f1, store, slot, phases);
+      default:
+        return mpm::launch_substep_bwd<double, double>(C, (const double*)state_f, (const double*)state_f1,
+                                                       (const double*)g_state_f1, (double*)g_state_f, pose_f,
+                                                       pose_f1, g_pose_f, g_pose_f1, store, slot, phases);
+    }
+  };
+  cudaError_t e = cudaSuccess;
+  if (!h->pipelined || h->prof.on) {  // the profiler times the kernels one at a time
+    e = run(L, mpm::BWD_ALL);
+    h->pipe_pending = false;
+  } else {
+    // The previous call left its p2g.grad queued on this stream after an
+    // event that follows its grid_op.grad.  This substep's preparation (block
+    // list, pose table, grids restored or recomputed) touches neither that
+    // kernel's inputs nor its outputs, so it runs on the side stream as soon
+    // as grid_op.grad is done, beside that p2g.grad; g2p.grad then waits for
+    // both.
+    const cudaStream_t main = (cudaStream_t)stream;
+    unsigned grid_phases = mpm::BWD_GRID;
+    if (h->pipe_pending && h->pipe_stream == stream) {
+      mpm::LaunchCtx S = L;
+      S.stream = h->pipe_side;
+      e = cudaStreamWaitEvent(h->pipe_side, h->pipe_grid_done, 0);
+      if (e == cudaSuccess) e = run(S, mpm::BWD_PREPARE);
+      if (e == cudaSuccess) e = cudaEventRecord(h->pipe_prep_done, h->pipe_side);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(main, h->pipe_prep_done, 0);
+      grid_phases |= mpm::BWD_G2P_PLAIN;  // the kernel before it on this stream is the previous p2g.grad
+    } else {
+      e = run(L, mpm::BWD_PREPARE);
+    }
+    if (e == cudaSuccess) e = run(L, grid_phases);
+    if (e == cudaSuccess) e = cudaEventRecord(h->pipe_grid_done, main);
+    if (e == cudaSuccess) e = run(L, mpm::BWD_PARTICLES);
+    h->pipe_pending = e == cudaSuccess;
+    h->pipe_stream = stream;
   }
   return e == cudaSuccess ? MPM_OK : cuda_fail(h, e, "mpm_substep_bwd");
+}
+
+int mpm_set_pipelined_adjoint(MpmHandle* h, int32_t on) {
+  if (!h) return fail(nullptr, MPM_E_INVALID, "mpm_set_pipelined_adjoint: NULL handle");
+  h->pipelined = on != 0;
+  h->pipe_pending = false;
+  return MPM_OK;
 }
 
 int mpm_set_chained(MpmHandle* h, int32_t on) {

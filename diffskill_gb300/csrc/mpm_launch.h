@@ -134,10 +134,17 @@ template <typename T, typename S>
 cudaError_t launch_substep_fwd(const LaunchCtx& L, const T* st0, T* st1, const double* pose_f,
                                const double* pose_f1, const MpmGridStore* store = nullptr, int slot = -1,
                                bool premarked = false, bool mark_next = false);
+// The adjoint substep in three phases, which a caller may issue on two
+// streams: BWD_PREPARE (active blocks, pose table, the grids restored from the
+// store or recomputed), BWD_GRID (g2p.grad, grid_op.grad) and BWD_PARTICLES
+// (p2g.grad).  BWD_G2P_PLAIN launches g2p.grad without the programmatic
+// dependency on the kernel before it.
+constexpr unsigned BWD_PREPARE = 1u, BWD_GRID = 2u, BWD_PARTICLES = 4u, BWD_G2P_PLAIN = 8u;
+constexpr unsigned BWD_ALL = BWD_PREPARE | BWD_GRID | BWD_PARTICLES;
 template <typename T, typename S>
 cudaError_t launch_substep_bwd(const LaunchCtx& L, const T* st0, const T* st1, const T* g1, T* g0, const double* pose_f,
                                const double* pose_f1, double* g_pose_f, double* g_pose_f1,
-                               const MpmGridStore* store = nullptr, int slot = -1);
+                               const MpmGridStore* store = nullptr, int slot = -1, unsigned phases = BWD_ALL);
 template <typename T>
 cudaError_t launch_grid_mass(const LaunchCtx& L, const T* st, T* gm);
 template <typename T>

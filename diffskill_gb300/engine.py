@@ -202,6 +202,12 @@ class MpmEngine:
         substeps (up to the per-scene re-sort) may be chained."""
         _lib.check(self.lib.mpm_set_chained(self.h, 1 if on else 0), self.h, "mpm_set_chained")
 
+    def set_pipelined_adjoint(self, on: bool) -> None:
+        """Pipelined adjoint substeps: each adjoint substep's grid preparation runs
+        on an internal stream beside the previous substep's p2g.grad.  Only
+        between adjoint substeps with no forward substep in between."""
+        _lib.check(self.lib.mpm_set_pipelined_adjoint(self.h, 1 if on else 0), self.h, "mpm_set_pipelined_adjoint")
+
     def substep(self, st0, st1, pose_f, pose_f1, store: "GridStore" = None, slot: int = -1) -> None:
         if store is None:
             _lib.check(self.lib.mpm_substep_fwd(self.h, _ptr(st0), _ptr(st1), _ptr(pose_f), _ptr(pose_f1),
@@ -646,6 +652,9 @@ class Horizon:
                                          None if self.coll is None else self.coll[s])
                 pending -= 1
 
+        # k == 1: no forward recompute between the adjoint substeps, so each one's
+        # grid preparation may run beside the previous one's p2g.grad
+        eng.set_pipelined_adjoint(k == 1)
         for c in range(self.F // k - 1, -1, -1):
             frames = [self.ckpt[c]]
             if store is not None and k > 1:
@@ -671,6 +680,7 @@ class Horizon:
                 cur, nxt = nxt, cur
             tools_bwd_upto(f0)
         tools_bwd_upto(0)
+        eng.set_pipelined_adjoint(False)
         if eng.T:
             main.wait_stream(self.side)
         self.g_state0 = cur

@@ -212,6 +212,19 @@ int mpm_substep_bwd(MpmHandle* h, const void* state_f, const void* state_f1, con
  * adjoint substep ends the chain.  No counterpart in the reference. */
 int mpm_set_chained(MpmHandle* h, int32_t on);
 
+/* Pipelined adjoint substeps (on = 1; off by default).  While on, an
+ * adjoint substep (mpm_substep_bwd / mpm_substep_bwd_store) that follows
+ * another on the same stream runs its grid preparation (active blocks, pose
+ * table, forward grids restored from the store or recomputed) on an internal
+ * stream, beside the previous substep's p2g.grad; its g2p.grad waits for both.
+ * Contract: between two such calls the caller's stream runs nothing that
+ * writes the handle's grids or pose table (no forward substep; a frame
+ * gradient permutation, the losses' adjoints and the tool kinematics adjoint
+ * are fine).  A forward substep, a change of stream or turning it off or on
+ * again ends the overlap.  The internal stream and its two events belong to
+ * the handle (created by mpm_create).  No counterpart in the reference. */
+int mpm_set_pipelined_adjoint(MpmHandle* h, int32_t on);
+
 /* Sets the launch shapes of the handle's later substeps (MpmTuning; a value
  * outside a field's candidates returns MPM_E_INVALID and changes nothing).
  * No counterpart in the reference. */

@@ -177,6 +177,45 @@ def test_checkpoint_recompute_equals_store_all(gpu_lib):
     assert rel_err(g2, g1) < 1e-9 and rel_err(g3, g1) < 1e-9
 
 
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 1e-4)])
+def test_pipelined_adjoint_equals_serial(gpu_lib, monkeypatch, prec, tol):
+    """Every frame kept (k=1): the adjoint substeps run pipelined (each one's
+    grid preparation beside the previous one's p2g.grad); loss, action and
+    initial-state gradients equal the serial adjoint's.  FP64 to 1e-12; FP32
+    to 1e-4, the run-to-run spread of its scatter's atomic summation order
+    over 40 substeps (measured 2e-5 on the initial-state gradient)."""
+    sc = small_scene(n=4000, n_actions=2, substeps=20, tools=[all_tools()[0], all_tools()[2]], precision=prec)
+    eng = make_engine(sc)
+    runs = []
+    for pipelined in (True, False):
+        if not pipelined:
+            real = eng.set_pipelined_adjoint
+            monkeypatch.setattr(eng, "set_pipelined_adjoint", lambda on: real(False))
+        l, g, hz = _traj(eng, sc, k=1)
+        runs.append((l, g, hz.g_state0[:, :sc.n_particles].clone()))
+    (l0, g0, s0), (l1, g1, s1) = runs
+    assert abs(l1 - l0) <= tol * abs(l0)
+    assert rel_err(g1, g0) < tol
+    assert rel_err(s1.cpu().numpy(), s0.cpu().numpy()) < tol
+
+
+def test_auto_checkpoint_interval_fits_the_budget_and_keeps_gradients(gpu_lib):
+    """ckpt_every="auto" under a frame budget of 16 frames: 40 substeps need 43
+    frames at k=1, so the planner takes k=4 (11 checkpoints + a 4-frame
+    segment); loss and action gradients equal the store-all run."""
+    sc = small_scene(n=3000, n_actions=2, substeps=20, precision="fp64")
+    eng = make_engine(sc)
+    l1, g1, _ = _traj(eng, sc, k=1)
+    frame_bytes = 24 * eng.ld * 8
+    hz = Horizon(eng, sc.n_actions, ckpt_every="auto", frame_budget_bytes=16 * frame_bytes)
+    assert hz.k == 4 and hz.n_ckpt == 11
+    hz.forward(eng.init_state([sc.x0]), eng.expand_actions([sc.actions]))
+    l2 = float(hz.loss(eng.targets([sc.target]), sc.density_weight, sc.contact_weight).sum())
+    g2 = eng.collapse_action_grad(hz.backward())[0].cpu().numpy()
+    assert abs(l2 - l1) <= 1e-12 * abs(l1)
+    assert rel_err(g2, g1) < 1e-9
+
+
 def test_batched_scenes_equal_single_scenes(gpu_lib):
     """Three scenes with different particle counts and tool sets in one launch
     give the same loss and action gradients as three separate runs."""
