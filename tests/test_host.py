@@ -104,6 +104,10 @@ def test_c_abi_rejects_bad_arguments_without_a_gpu():
     assert lib.mpm_create(ctypes.byref(p), offs, ctypes.byref(h)) == 1
     assert "multiple of 8" in _lib.last_error(None)
     assert lib.mpm_substep_fwd(None, None, None, None, None, None) == 1
+    assert lib.mpm_sort_frame(None, None, None, None, None) == 1
+    assert "NULL handle" in _lib.last_error(None)
+    assert lib.mpm_unsort_frame(None, None, None, None, None) == 1
+    assert lib.mpm_set_pipelined_adjoint(None, 1) == 1
 
 
 def test_shard_scenes_balances_and_covers():
