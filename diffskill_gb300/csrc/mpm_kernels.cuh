@@ -310,6 +310,16 @@ MPM_DI long long cell_key(const Consts<T>& c, int scene, const Stencil<T>& s) {
   return (long long)scene * c.G + ((long long)s.base[0] * c.n_grid + s.base[1]) * c.n_grid + s.base[2];
 }
 
+// Loads issued before a kernel's pdl_wait() go to L2 (ld.global.cg): a
+// dependent launch may start on an SM whose L1 still holds lines of an older
+// content of the same buffer, and only the wait makes the earlier kernels'
+// writes visible through L1.  L2 is coherent, and everything these loads read
+// was written by kernels that completed before this one started.
+template <typename T>
+MPM_DI void load_row_cg(const T* __restrict__ st, int64_t ld, int64_t p, int r0, int n, T* out) {
+#pragma unroll
+  for (int k = 0; k < n; ++k) out[k] = __ldcg(st + (int64_t)(r0 + k) * ld + p);
+}
 template <typename T>
 MPM_DI void load_row(const T* __restrict__ st, int64_t ld, int64_t p, int r0, int n, T* out) {
 #pragma unroll
@@ -725,14 +735,14 @@ MPM_DI void p2g_chunk(const Consts<T>& c, const T* __restrict__ st, T* __restric
   if (valid) {
     T x[3], v[3];
     S C[9], F[9];
-    load_row(st, c.ld, p, 0, 3, x);
-    load_row(st, c.ld, p, 3, 3, v);
+    load_row_cg(st, c.ld, p, 0, 3, x);
+    load_row_cg(st, c.ld, p, 3, 3, v);
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      C[k] = S(st[(int64_t)(6 + k) * c.ld + p]);
-      F[k] = S(st[(int64_t)(15 + k) * c.ld + p]);
+      C[k] = S(__ldcg(st + (int64_t)(6 + k) * c.ld + p));
+      F[k] = S(__ldcg(st + (int64_t)(15 + k) * c.ld + p));
     }
-    const int sc = pscene[p];  // issued with the state rows
+    const int sc = __ldcg(pscene + p);  // issued with the state rows
     ok = make_stencil(c, x, s);
     MatConsts<S> m = mat_consts<T, S>(c);
     P2G<S> P;
@@ -854,7 +864,7 @@ template <typename T, typename S, bool Strided = false, int MB = 0>
 __global__ void __launch_bounds__(128, MB > 0 ? MB : ((sizeof(T) == 4 && sizeof(S) == 4) ? 7 : 4)) k_p2g(Consts<T> c, const T* __restrict__ st, T* __restrict__ st_out,
                                              const int* __restrict__ pscene, Node<T>* __restrict__ grid,
                                              const int64_t* __restrict__ saved) {
-  if (saved && *saved >= 0) {  // the grid of this substep was restored from the grid store
+  if (saved && __ldcg(saved) >= 0) {  // the grid of this substep was restored from the grid store
     pdl_wait();  // completes only after the kernel before it (dependent launches chain through it)
     return;
   }
@@ -1039,11 +1049,11 @@ template <typename T>
 MPM_DI bool g2p_particle(const Consts<T>& c, const T* __restrict__ st, T* __restrict__ st_out, int64_t p, int scene,
                          const Node<T>* __restrict__ grid, T* xn) {
   T x[3];
-  load_row(st, c.ld, p, 0, 3, x);
+  load_row_cg(st, c.ld, p, 0, 3, x);
   Stencil<T> s;
   if (!make_stencil(c, x, s)) {  // flagged by k_p2g; the particle keeps its state
 #pragma unroll
-    for (int k = 0; k < 15; ++k) st_out[(int64_t)k * c.ld + p] = st[(int64_t)k * c.ld + p];
+    for (int k = 0; k < 15; ++k) st_out[(int64_t)k * c.ld + p] = __ldcg(st + (int64_t)k * c.ld + p);
     return false;
   }
   const Node<T>* g = grid + (int64_t)scene * c.G;
@@ -1102,7 +1112,7 @@ __global__ void __launch_bounds__(128, MB > 0 ? MB : (sizeof(T) == 4 ? 8 : 1)) k
                                              unsigned char* __restrict__ mark, int* __restrict__ header) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = p < c.n_particles;
-  const int scene = valid ? pscene[p] : 0;  // issued with x
+  const int scene = valid ? __ldcg(pscene + p) : 0;  // issued with x
   T xn[3] = {T(0), T(0), T(0)};
   const bool moved = valid && g2p_particle(c, st, st_out, p, scene, grid, xn);
   pdl_wait();  // grid_op reads the header reset below (and lanes without a stencil have not waited)
@@ -1146,12 +1156,12 @@ __global__ void __launch_bounds__(128, MB > 0 ? MB : (sizeof(T) == 4 ? 6 : 2)) k
   for (int k = 0; k < 9; ++k) gC[k] = T(0);
   if (valid) {
     // every row this particle needs is requested together with x
-    load_row(st, c.ld, p, 0, 3, x);
-    if (st1) load_row(st1, c.ld, p, 3, 3, nv);
-    load_row(g1, c.ld, p, 0, 3, gx1);
-    load_row(g1, c.ld, p, 3, 3, gnv);
-    load_row(g1, c.ld, p, 6, 9, gC);
-    scene = pscene[p];
+    load_row_cg(st, c.ld, p, 0, 3, x);
+    if (st1) load_row_cg(st1, c.ld, p, 3, 3, nv);
+    load_row_cg(g1, c.ld, p, 0, 3, gx1);
+    load_row_cg(g1, c.ld, p, 3, 3, gnv);
+    load_row_cg(g1, c.ld, p, 6, 9, gC);
+    scene = __ldcg(pscene + p);
     ok = make_stencil(c, x, s);
     if (!ok) {
       zero_stencil(s);
@@ -1433,14 +1443,14 @@ __global__ void __launch_bounds__(128, MB > 0 ? MB : ((sizeof(T) == 4 && sizeof(
   for (int k = 15; k < 24; ++k) prefetch_l2(g1 + (int64_t)k * c.ld + p);
   T x[3], v[3];
   S C[9], F[9];
-  load_row(st, c.ld, p, 0, 3, x);
-  load_row(st, c.ld, p, 3, 3, v);
+  load_row_cg(st, c.ld, p, 0, 3, x);
+  load_row_cg(st, c.ld, p, 3, 3, v);
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
-    C[k] = S(st[(int64_t)(6 + k) * c.ld + p]);
-    F[k] = S(st[(int64_t)(15 + k) * c.ld + p]);
+    C[k] = S(__ldcg(st + (int64_t)(6 + k) * c.ld + p));
+    F[k] = S(__ldcg(st + (int64_t)(15 + k) * c.ld + p));
   }
-  const int scene = pscene[p];  // issued with the state rows
+  const int scene = __ldcg(pscene + p);  // issued with the state rows
   Stencil<T> s;
   bool ok = make_stencil(c, x, s);
   MatConsts<S> m = mat_consts<T, S>(c);
@@ -1451,7 +1461,7 @@ __global__ void __launch_bounds__(128, MB > 0 ? MB : ((sizeof(T) == 4 && sizeof(
 #pragma unroll
   for (int k = 0; k < 9; ++k) affine[k] = T(aff[k]);
   T gx[3], gv[3] = {T(0), T(0), T(0)};
-  load_row(g0, c.ld, p, 0, 3, gx);
+  load_row_cg(g0, c.ld, p, 0, 3, gx);
   S g_aff[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) g_aff[k] = S(0);
