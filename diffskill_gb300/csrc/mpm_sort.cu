@@ -19,10 +19,10 @@
 // stably (a warp takes 4 rounds of 32 consecutive keys; peers of one digit
 // are found with __match_any_sync).  Tiles of 1024 keys rather than 4096 put
 // four times as many CTAs on the SMs (re-sort of 1.2M particles 116.8 ->
-// 108.9 us).  Ties keep their original order,
-// so the permutation is deterministic.  The 24 rows of the frame are then
-// gathered once through the permutation into the destination frame; the
-// adjoint scatters a frame gradient back through the same permutation.
+// 108.9 us).  Ties keep their original order, so the permutation is
+// deterministic.  The 24 rows of the frame are then gathered once through
+// the permutation into the destination frame; the adjoint scatters a frame
+// gradient back through the same permutation.
 #include "mpm_kernels.cuh"
 #include "mpm_launch.h"
 
